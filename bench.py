@@ -1,0 +1,443 @@
+"""Benchmark of the Fletcher TTI time step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (BASELINE configs[1]): 512^3 interior + 48-cell absorbing shell
+(616^3 padded, 608^3 = 224.8 M updated points per step), dt = 0.8 ms,
+dx = dy = dz = 12.5 m, seeded 12-layer medium (numpy PCG64 seed 2026) on the
+GPU, 20 Hz Ricker (FCUT = 60) at interior depth 20, 48-cell sponge.  A step
+is one time step of the whole cube; K = 2000 steps is the config's length.
+The working set (14 x 0.93 GB) is far larger than the 129 MB L2, so no L2
+flush is needed between steps.
+
+Metric: point-updates per second (compute region x steps / time), the
+reference's MSamples/s divided by 1000 (reference src/main.c:207-214).
+
+Our arm: ``value`` is the device-resident rate (graph-replayed steps, CUDA
+events on the library's stream); ``e2e`` is the same rate through the
+reference-facing C ABI with host buffers (dc_device_data_init with the
+copies, dc_device_add_source + dc_propagate + dc_device_swap_arrays per
+step, dc_device_data_get_results), wall clock.  ``roofline`` compares the
+stencil kernel's algorithmic bytes (64 B per update) per launch time with the
+measured HBM copy bandwidth; ``cpu_baseline`` times the CPU oracle on a
+bounded slab of the same workload.
+
+Reference arm (--impl reference): the reference's CPU implementation of the
+path (the oracle port of src/openmp_propagate.c, all host threads) on the
+same workload; each step is one time step of a 608 x 608 x 16 slab.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "TTI Gpoint-updates/s & %HBM roofline: plain vs mixed/batched/learned at stated L2"
+UNIT = "Gpoint-updates/s"
+N_INTERIOR, ABSORB = 512, 48
+DT, DX = 0.8e-3, 12.5
+FCUT = 60.0           # Ricker peak fcut/3 = 20 Hz
+SRC_DEPTH = 20        # interior-relative depth of the source (cells)
+MEDIUM_SEED = 2026
+SPONGE_KAPPA = 0.35
+BYTES_PER_UPDATE = 64  # pc,qc,pp,qp + 10 coefficients read, pp,qp written
+SLAB_PLANES = 16       # CPU sample: planes per step
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--kernel", choices=("fast", "exact"), default="fast")
+    ap.add_argument("--n", type=int, default=N_INTERIOR, help="interior cells per axis")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(name: str):
+    """DRAM bytes per point-update of the stencil kernel from the committed
+    ncu summary (a line 'traffic_bytes_per_update: X'), or None."""
+    f = ROOT / "profiles" / name
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_update:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def geometry(n: int):
+    from dc_gb300.medium import Geometry
+    return Geometry((n, n, n), ABSORB)
+
+
+def shot_source(geom, rank: int) -> int:
+    """Rank r runs shot r: sources step along x from the centre (weak scaling:
+    one independent shot per GPU, shared medium, no exchange)."""
+    sx, sy, _ = geom.sizes
+    o = 4 + geom.absorb
+    x = sx // 2 + (rank * 16) % max(1, geom.n[0] // 2)
+    return geom.index(x, sy // 2, o + SRC_DEPTH)
+
+
+def make_spec(geom):
+    from dc_gb300 import medium
+    return medium.layered_spec(MEDIUM_SEED, geom.sizes)
+
+
+def slab_inputs(dc, port, geom, planes: int):
+    """Host inputs of a CPU sample: a z-slab of the workload (full x-y
+    extent, `planes` updated planes around the source depth) with its medium
+    precomputed like the reference (src/precomp.c:85-105)."""
+    from dc_gb300 import medium
+    sx, sy, sz = geom.sizes
+    z0 = 4 + geom.absorb + SRC_DEPTH - planes // 2 - 4
+    spec = medium.with_origin(make_spec(geom), (0, 0, z0))
+    sizes = (sx, sy, planes + 8)
+    aniso = medium.layered_fields(spec, sizes)
+    coef = port.precomp(aniso)
+    rng = np.random.Generator(np.random.PCG64(1))
+    shape = (sizes[2], sy, sx)
+    fields = [(rng.standard_normal(shape) * 1e-3).astype(np.float32) for _ in range(4)]
+    return sizes, coef, fields
+
+
+def time_cpu_oracle(port, sizes, coef, fields, target_s: float, nthreads: int):
+    """Repeated oracle steps over the slab until ~target_s; returns
+    (updates/s, steps, seconds)."""
+    from oracle.oracle import KIND_F32
+    sx, sy, sz = sizes
+    pc, qc, pp, qp = fields
+    b0, b1 = (4, 4, 4), (sx - 4, sy - 4, sz - 4)
+    pts = (sx - 8) * (sy - 8) * (sz - 8)
+    t0 = time.perf_counter()
+    port.step(KIND_F32, sizes, b0, b1, (DX,) * 3, DT, pc, qc, pp, qp, coef=coef, nthreads=nthreads)
+    one = time.perf_counter() - t0
+    reps = max(1, int(target_s / max(one, 1e-6)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        port.step(KIND_F32, sizes, b0, b1, (DX,) * 3, DT, pc, qc, pp, qp, coef=coef,
+                  nthreads=nthreads)
+    el = time.perf_counter() - t0
+    return pts * reps / el, reps, el
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    """Reference arm: the CPU implementation of the path on the host cores."""
+    if rank != 0:
+        return
+    from oracle import build_oracle
+    from oracle.oracle import KIND_F32, Port
+    import __graft_entry__ as ge
+    dc = ge.package()
+    geom = geometry(args.n)
+    port = Port()
+    nthreads = os.cpu_count() or 1
+    kind = "port"
+    sizes, coef, fields = slab_inputs(dc, port, geom, SLAB_PLANES)
+    sx, sy, sz = sizes
+    pc, qc, pp, qp = fields
+    b0, b1 = (4, 4, 4), (sx - 4, sy - 4, sz - 4)
+    pts = (sx - 8) * (sy - 8) * (sz - 8)
+    for _ in range(args.warmup):
+        port.step(KIND_F32, sizes, b0, b1, (DX,) * 3, DT, pc, qc, pp, qp, coef=coef,
+                  nthreads=nthreads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        port.step(KIND_F32, sizes, b0, b1, (DX,) * 3, DT, pc, qc, pp, qp, coef=coef,
+                  nthreads=nthreads)
+        pp, pc = pc, pp
+        qp, qc = qc, qp
+    el = time.perf_counter() - t0
+    value = pts * args.steps / el / 1e9
+    sample = (f"{args.steps} steps of the {sx - 8}x{sy - 8}x{sz - 8} updated slab "
+              f"(full x-y extent of the {geom.sizes[0]}^3 cube around the source depth)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded layered medium, numpy PCG64 seed 2026)",
+        "config": {"workload": f"plain FP32 TTI, {args.n}^3 interior + {ABSORB} absorbing, "
+                               f"slab sample of {SLAB_PLANES} planes", "global_batch": 1,
+                   "seq_len": None, "parallelism": "cpu", "threads": nthreads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, local):
+    import torch
+    import __graft_entry__ as ge
+    dc = ge.package()
+    dc.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(v: float) -> float:
+        if dist is None:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    geom = geometry(args.n)
+    sizes = geom.sizes
+    pts = geom.compute_points
+    kernel = dc.KERNEL_FAST if args.kernel == "fast" else dc.KERNEL_EXACT
+    total_steps = args.warmup + args.steps
+    src_amp = dc.source_table(DT, total_steps + 1, FCUT)
+    src_idx = shot_source(geom, rank)
+    sponge = [dc.sponge_profile(s, geom.absorb, SPONGE_KAPPA) for s in sizes]
+
+    # ---- device-resident run (value, roofline) -------------------------
+    sim = dc.Simulation(sizes, (DX,) * 3, DT, kernel=kernel, medium=dc.MEDIUM_PRECOMP,
+                        device=local)
+    sim.generate_layered(make_spec(geom))
+    sim.set_fields()
+    sim.set_source(src_idx, src_amp)
+    sim.set_sponge(*sponge)
+    sim.run(args.warmup)
+    sim.synchronize()
+    stream = torch.cuda.ExternalStream(sim.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = sim.launches
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        sim.run(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    sim.synchronize()
+    launches = sim.launches - l0
+    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(ms)
+    barrier()
+    value = pts * args.steps * world / (ms * 1e-3) / 1e9
+    stencil_ms = ms / args.steps  # graph-replayed region: one stencil launch per step
+    achieved = BYTES_PER_UPDATE * pts / (stencil_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    traffic_pp = profiled_traffic("tti_fast_config2.md") if kernel == dc.KERNEL_FAST else None
+    out_fields = sim.get_fields() if not args.no_cpu_baseline else None
+    sim.close()
+
+    # ---- end to end through the reference ABI with host buffers ----------
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_over_ranks,
+                      world)
+
+    # ---- CPU baseline: the oracle on a slab (rank 0, N = 1) ---------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle.oracle import Port
+        port = Port()
+        nthreads = os.cpu_count() or 1
+        ssizes, coef, fields = slab_inputs(dc, port, geom, SLAB_PLANES)
+        rate, reps, el = time_cpu_oracle(port, ssizes, coef, fields, 12.0, nthreads)
+        cpu = {"value": rate / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"{reps} oracle steps of a {ssizes[0] - 8}x{ssizes[1] - 8}x"
+                         f"{ssizes[2] - 8} slab of the same workload ({el:.1f} s)"}
+        del out_fields
+
+    if rank != 0:
+        return
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded 12-layer TTI medium, numpy PCG64 seed 2026, generated on GPU)",
+        "config": {"workload": f"plain FP32 TTI, {args.n}^3 interior + {ABSORB}-cell sponge, "
+                               f"{geom.sizes[0]}^3 padded, dt 0.8 ms, 20 Hz Ricker",
+                   "kernel": args.kernel, "points_per_step": pts, "global_batch": world,
+                   "seq_len": None, "parallelism": f"shots{world}" if world > 1 else "single",
+                   "l2": "inputs 13 GB >> 129 MB L2; no flush"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "bytes_per_update": BYTES_PER_UPDATE,
+                     "traffic": (traffic_pp * pts) if traffic_pp else None},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_over_ranks, world):
+    """Same workload through the reference's entry points with host
+    buffers: the medium comes from pinned host arrays, the loop is
+    src/worker.c's (source, propagate, swap), results come back to the
+    host.  Wall clock around everything."""
+    sizes = geom.sizes
+    sx, sy, sz = sizes
+    shape = (sz, sy, sx)
+    pts = geom.compute_points
+
+    def pinned(n_floats):
+        t = torch.empty(n_floats, dtype=torch.float32, pin_memory=True)
+        return t, t.numpy()
+
+    # build the host medium once (outside the timed region): generate on the
+    # GPU, copy to pinned host memory
+    n = sx * sy * sz
+    keep = []
+    coef_host = []
+    for _ in dc.COEF_NAMES:
+        t, a = pinned(n)
+        keep.append(t)
+        coef_host.append(a.reshape(shape))
+    gen = dc.Simulation(sizes, (DX,) * 3, DT, kernel=kernel, device=local)
+    gen.generate_layered(make_spec(geom))
+    gen.get_precomp(coef_host)
+    gen.close()
+    fields = []
+    for _ in range(4):
+        t, a = pinned(n)
+        a[:] = 0.0
+        keep.append(t)
+        fields.append(a.reshape(shape))
+    os.environ["DC_GB300_KERNEL"] = args.kernel
+    os.environ["DC_GB300_DEVICE"] = str(local)
+    proc = dc.Process(sizes, (DX,) * 3, DT, pp=None, pc=None, qp=None, qc=None,
+                      precomp=coef_host, source_index=src_idx)
+    # Process copies its field arrays; point pc/qc at pinned outputs instead
+    for name, arr in zip(("pp", "pc", "qp", "qc"), fields):
+        proc._keep[name] = arr
+        setattr(proc.proc, name, dc.fptr(arr))
+    amp = [dc.source(DT, i, FCUT) for i in range(args.steps + 1)]
+    b0 = (4, 4, 4)
+    b1 = (sx - 4, sy - 4, sz - 4)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    data = dc.device_data_init(proc)
+    for it in range(args.steps):
+        dc.device_add_source(data, src_idx, amp[it])
+        dc.propagate(b0, b1, sizes, data, DX, DX, DX, DT)
+        dc.device_swap_arrays(data)
+    dc.device_data_get_results(proc, data)
+    el = time.perf_counter() - t0
+    dc.device_data_free(data)
+    el = max_over_ranks(el)
+    h2d = 14 * sx * sy * sz * 4
+    d2h = 2 * sx * sy * sz * 4
+    return {"value": pts * args.steps * world / el / 1e9, "unit": UNIT,
+            "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+            "seconds": el, "api": "reference C ABI (dc_device_data_init, dc_device_add_source, "
+                                  "dc_propagate, dc_device_swap_arrays, "
+                                  "dc_device_data_get_results), pinned host buffers"}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

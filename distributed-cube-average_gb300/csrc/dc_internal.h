@@ -1,0 +1,164 @@
+// dc_internal.h -- internal declarations shared by the CUDA translation
+// units of libdc_gb300.so.  Not part of the public ABI (include/dc_gb300.h).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "dc_gb300.h"
+
+namespace dcg {
+
+// ---------------------------------------------------------------------------
+// Finite-difference coefficients: 8th-order central differences of the
+// reference (include/derivatives.h:15-38), as exact rationals rounded once
+// (they round to the same floats as the reference's decimal literals).
+// ---------------------------------------------------------------------------
+#define DCG_K0 (-205.0f / 72.0f)
+#define DCG_K1 (8.0f / 5.0f)
+#define DCG_K2 (-1.0f / 5.0f)
+#define DCG_K3 (8.0f / 315.0f)
+#define DCG_K4 (-1.0f / 560.0f)
+#define DCG_L1 (4.0f / 5.0f)
+#define DCG_L2 (-1.0f / 5.0f)
+#define DCG_L3 (4.0f / 105.0f)
+#define DCG_L4 (-1.0f / 280.0f)
+
+// Order of the coefficient arrays inside the device medium block.  The
+// three in-plane coefficients come first so one TMA box fetches them at the
+// leading plane and a second box the other seven at the output plane.
+enum DevCoef {
+  DC_CXX = 0, DC_CYY, DC_CXY, DC_CZZ, DC_CXZ, DC_CYZ,
+  DC_V2PX, DC_V2PZ, DC_V2SZ, DC_V2PN, DC_NCOEF
+};
+// Device slot of each dc_precomp_vars field (reference order ch1dxx, ch1dyy,
+// ch1dzz, ch1dxy, ch1dyz, ch1dxz, v2px, v2pz, v2sz, v2pn).
+constexpr int kRefToDev[10] = {DC_CXX, DC_CYY, DC_CZZ, DC_CXY, DC_CYZ,
+                               DC_CXZ, DC_V2PX, DC_V2PZ, DC_V2SZ, DC_V2PN};
+
+constexpr int kHalo = 4;  // stencil radius (include/definitions.h:4)
+
+// Error word bits written by kernels.
+enum : int { kErrTimeout = 1 };
+
+struct StepParams {
+  int x0, x1, y0, y1, z0, z1;   // half-open box of updated points
+  int tile_x0, tile_y0;         // origin of the block grid (tile_x0 % 4 == 0)
+  int zchunk;                   // output planes per block
+  long long pitch, plane;       // floats between rows / planes
+  float dxxinv, dyyinv, dzzinv, dxyinv, dxzinv, dyzinv;
+  float dt, dt2;
+  float *pp_out, *qp_out;       // pp/qp buffers (read, then written in place)
+  const float *pc_in, *qc_in;   // current fields (exact kernel reads these)
+  const float *coef;            // [DC_NCOEF][count]
+  const float *vv;              // [2][count]: vpz, vsv (VPZ_VSV medium)
+  long long count;              // floats per array (incl. pitch padding)
+  const float *sponge;          // gx[sx] | gy[sy] | gz[sz], or null
+  int sponge_oy, sponge_oz;     // offsets of gy / gz in `sponge`
+  // fused source: the value added when storing step `step` is
+  // src_table[step + 1] (it becomes pc of the next step)
+  int src_x, src_y, src_z;      // src_x < 0: none
+  const float *src_table;
+  int src_count;
+  const int *d_step;            // device step counter (graph replays)
+  int step_offset;              // step = *d_step + step_offset
+  float *src_pre;               // p,q at the source point before injection
+  // fused energy: sum(p^2+q^2) of the new fields, one double per step
+  double *energy;
+  int energy_cap;
+  int *err;
+};
+
+struct Sim {
+  dc_gb300_sim *handle = nullptr;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  long long sx = 0, sy = 0, sz = 0, pitch = 0, plane = 0, count = 0;
+  float dx = 0, dy = 0, dz = 0, dt = 0;
+  int kernel = DC_GB300_KERNEL_FAST;
+  int medium = DC_GB300_MEDIUM_PRECOMP;
+  float *field[4] = {nullptr, nullptr, nullptr, nullptr};
+  float *coef = nullptr;       // [DC_NCOEF][count]
+  float *vv = nullptr;         // [2][count]
+  float *sponge = nullptr;     // [sx + sy + sz]
+  bool has_sponge = false;
+  // source
+  long long src_gi = -1;
+  int src_x = -1, src_y = -1, src_z = -1;
+  float *d_src = nullptr;
+  int src_count = 0;
+  long long src_applied_step = -1;  // pc already holds src(step) for it
+  float *d_src_pre = nullptr;
+  // receivers
+  long long *d_rec = nullptr;
+  int nrec = 0;
+  float *d_traces = nullptr;
+  int trace_cap = 0;
+  // energy
+  double *d_energy = nullptr;
+  int energy_cap = 0;
+  // counters and status
+  int *d_step = nullptr;
+  long long steps_done = 0;
+  int *d_err = nullptr;
+  long long launches = 0;
+  int config_version = 0;
+  // tensor maps for the fast kernel (encoded for one tile shape)
+  CUtensorMap tm_halo[4], tm_own[4], tm_ca, tm_cb;
+  int maps_tx = 0, maps_ty = 0;
+  // captured multi-step graphs, keyed by start parity of the pc buffer
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int graph_steps[2] = {0, 0};
+  int graph_version[2] = {-1, -1};
+  int graph_pc[2] = {-1, -1};
+};
+
+// Fast-kernel tile geometry (chosen at compile time; see tti_fast.cu).
+struct FastShape {
+  int tx, ty, zchunk;
+};
+FastShape fast_shape(const Sim *sim);
+bool fast_encode_maps(Sim *sim, std::string *err);
+
+// Launchers.  Return the cudaError_t of the launch.
+cudaError_t launch_fast(Sim *sim, const StepParams &prm, int pc_buf,
+                        int qc_buf, int pp_buf, int qp_buf);
+cudaError_t launch_exact(Sim *sim, const StepParams &prm);
+cudaError_t launch_add_source(cudaStream_t st, float *pc, float *qc,
+                              long long gi, const float *table, int count,
+                              const int *d_step, int step_offset);
+cudaError_t launch_add_value(cudaStream_t st, float *pc, float *qc,
+                             long long gi, float value);
+cudaError_t launch_gather(cudaStream_t st, const float *p,
+                          const long long *idx, int n, float *traces, int cap,
+                          const int *d_step, int step_offset,
+                          long long src_gi, const float *src_pre);
+cudaError_t launch_advance_step(cudaStream_t st, int *d_step, int by);
+cudaError_t launch_precomp(cudaStream_t st, const float *theta,
+                           const float *phi, const float *vsv,
+                           const float *vpz, const float *eps,
+                           const float *delta, float *coef, long long count,
+                           long long n);
+cudaError_t launch_layered(cudaStream_t st, const dc_gb300_layered_spec &spec,
+                           float *coef, float *vv, long long sx, long long sy,
+                           long long sz, long long pitch, long long count);
+
+// Tensor-map encoding through the driver entry point (no -lcuda needed).
+bool encode_tiled(CUtensorMap *map, const void *base, int rank,
+                  const uint64_t *dims, const uint64_t *strides_bytes,
+                  const uint32_t *box, std::string *err);
+
+// Thread-local error text for dc_gb300_last_error().
+void set_error(const std::string &msg);
+
+}  // namespace dcg
+
+// The simulation handle.  `abi` must stay the first member: the reference
+// ABI hands out &handle->abi and dc_gb300_from_device_data() casts back.
+struct dc_gb300_sim {
+  dc_device_data abi;
+  dcg::Sim *impl;
+};

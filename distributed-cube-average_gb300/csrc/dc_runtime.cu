@@ -1,0 +1,953 @@
+// dc_runtime.cu -- simulation object, device memory, graph-captured time
+// loop, and the reference's device-data / propagate entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dc_internal.h"
+
+namespace dcg {
+
+namespace {
+thread_local std::string g_err;
+constexpr int kGraphChunk = 64;  // steps per captured graph (even)
+constexpr int kExactZChunk = 16;
+}  // namespace
+
+void set_error(const std::string &msg) { g_err = msg; }
+
+namespace {
+
+#define DCG_TRY(call)                                                       \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess) {                                                \
+      set_error(std::string(#call) + ": " + cudaGetErrorString(e_));       \
+      return DC_GB300_ERR_CUDA;                                             \
+    }                                                                       \
+  } while (0)
+
+int fail(int code, const std::string &msg) {
+  set_error(msg);
+  return code;
+}
+
+long long round_up4(long long v) { return (v + 3) / 4 * 4; }
+
+Sim *impl(dc_gb300_sim *h) { return h ? h->impl : nullptr; }
+
+// Copies a dense host array (sx*sy*sz) into a pitched device array.
+cudaError_t upload_dense(Sim *s, float *dst, const float *src) {
+  return cudaMemcpy2DAsync(dst, s->pitch * 4, src, s->sx * 4, s->sx * 4,
+                           s->sy * s->sz, cudaMemcpyHostToDevice, s->stream);
+}
+
+cudaError_t download_dense(Sim *s, float *dst, const float *src) {
+  return cudaMemcpy2DAsync(dst, s->sx * 4, src, s->pitch * 4, s->sx * 4,
+                           s->sy * s->sz, cudaMemcpyDeviceToHost, s->stream);
+}
+
+int buffer_of(const Sim *s, const float *p) {
+  for (int b = 0; b < 4; ++b)
+    if (s->field[b] == p) return b;
+  return -1;
+}
+
+// Keeps the reference-ABI view in step with the device arrays.
+void refresh_abi(Sim *s) {
+  dc_device_data &a = s->handle->abi;
+  a.vpz = s->vv;
+  a.vsv = s->vv ? s->vv + s->count : nullptr;
+  dc_precomp_vars &p = a.precomp_vars;
+  float *c = s->coef;
+  p.ch1dxx = c ? c + DC_CXX * s->count : nullptr;
+  p.ch1dyy = c ? c + DC_CYY * s->count : nullptr;
+  p.ch1dzz = c ? c + DC_CZZ * s->count : nullptr;
+  p.ch1dxy = c ? c + DC_CXY * s->count : nullptr;
+  p.ch1dyz = c ? c + DC_CYZ * s->count : nullptr;
+  p.ch1dxz = c ? c + DC_CXZ * s->count : nullptr;
+  p.v2px = c ? c + DC_V2PX * s->count : nullptr;
+  p.v2pz = c ? c + DC_V2PZ * s->count : nullptr;
+  p.v2sz = c ? c + DC_V2SZ * s->count : nullptr;
+  p.v2pn = c ? c + DC_V2PN * s->count : nullptr;
+}
+
+void drop_graphs(Sim *s) {
+  for (int i = 0; i < 2; ++i) {
+    if (s->graph[i]) cudaGraphExecDestroy(s->graph[i]);
+    s->graph[i] = nullptr;
+    s->graph_version[i] = -1;
+  }
+}
+
+void release(Sim *s) {
+  if (!s) return;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  drop_graphs(s);
+  for (float *&f : s->field) {
+    cudaFree(f);
+    f = nullptr;
+  }
+  cudaFree(s->coef);
+  cudaFree(s->vv);
+  cudaFree(s->sponge);
+  cudaFree(s->d_src);
+  cudaFree(s->d_src_pre);
+  cudaFree(s->d_rec);
+  cudaFree(s->d_traces);
+  cudaFree(s->d_energy);
+  cudaFree(s->d_step);
+  cudaFree(s->d_err);
+  if (s->stream) cudaStreamDestroy(s->stream);
+}
+
+// Fills the parameters of one stencil pass over a box.
+StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
+                       float dx, float dy, float dz, float dt) {
+  StepParams p{};
+  p.x0 = static_cast<int>(b0[0]);
+  p.x1 = static_cast<int>(b1[0]);
+  p.y0 = static_cast<int>(b0[1]);
+  p.y1 = static_cast<int>(b1[1]);
+  p.z0 = static_cast<int>(b0[2]);
+  p.z1 = static_cast<int>(b1[2]);
+  p.tile_x0 = p.x0 & ~3;
+  p.tile_y0 = p.y0;
+  p.zchunk = s->kernel == DC_GB300_KERNEL_FAST ? fast_shape(s).zchunk : kExactZChunk;
+  p.pitch = s->pitch;
+  p.plane = s->plane;
+  // include/sample_compute.h:40-45 (float, IEEE division)
+  p.dxxinv = 1.0f / (dx * dx);
+  p.dyyinv = 1.0f / (dy * dy);
+  p.dzzinv = 1.0f / (dz * dz);
+  p.dxyinv = 1.0f / (dx * dy);
+  p.dxzinv = 1.0f / (dx * dz);
+  p.dyzinv = 1.0f / (dy * dz);
+  p.dt = dt;
+  p.dt2 = dt * dt;
+  const dc_device_data &a = s->handle->abi;
+  p.pp_out = a.pp;
+  p.qp_out = a.qp;
+  p.pc_in = a.pc;
+  p.qc_in = a.qc;
+  p.coef = s->coef;
+  p.vv = s->vv;
+  p.count = s->count;
+  p.sponge = nullptr;
+  p.src_x = -1;
+  p.src_y = -1;
+  p.src_z = -1;
+  p.d_step = s->d_step;
+  p.src_pre = s->d_src_pre;
+  p.err = s->d_err;
+  return p;
+}
+
+cudaError_t launch_pass(Sim *s, const StepParams &p) {
+  ++s->launches;
+  if (s->kernel == DC_GB300_KERNEL_EXACT) return launch_exact(s, p);
+  const dc_device_data &a = s->handle->abi;
+  return launch_fast(s, p, buffer_of(s, a.pc), buffer_of(s, a.qc),
+                     buffer_of(s, a.pp), buffer_of(s, a.qp));
+}
+
+void swap_roles(dc_device_data *a) {
+  std::swap(a->pp, a->pc);
+  std::swap(a->qp, a->qc);
+}
+
+// Queues one full time step (j-th of a run): fused source for the next
+// step, stencil over [4, s-4)^3, receiver gather; then swaps the roles.
+cudaError_t queue_step(Sim *s, int j) {
+  const long long b0[3] = {4, 4, 4};
+  const long long b1[3] = {s->sx - 4, s->sy - 4, s->sz - 4};
+  StepParams p = make_params(s, b0, b1, s->dx, s->dy, s->dz, s->dt);
+  p.step_offset = j;
+  if (s->has_sponge) {
+    p.sponge = s->sponge;
+    p.sponge_oy = static_cast<int>(s->sx);
+    p.sponge_oz = static_cast<int>(s->sx + s->sy);
+  }
+  if (s->src_gi >= 0) {
+    p.src_x = s->src_x;
+    p.src_y = s->src_y;
+    p.src_z = s->src_z;
+    p.src_table = s->d_src;
+    p.src_count = s->src_count;
+  }
+  p.energy = s->d_energy;
+  p.energy_cap = s->energy_cap;
+  cudaError_t e = launch_pass(s, p);
+  if (e != cudaSuccess) return e;
+  if (s->nrec > 0) {
+    ++s->launches;
+    const long long src_gi = s->src_gi;
+    e = launch_gather(s->stream, s->handle->abi.pp, s->d_rec, s->nrec,
+                      s->d_traces, s->trace_cap, s->d_step, j, src_gi,
+                      s->d_src_pre);
+    if (e != cudaSuccess) return e;
+  }
+  swap_roles(&s->handle->abi);
+  return cudaSuccess;
+}
+
+int check_err_word(Sim *s) {
+  int h = 0;
+  DCG_TRY(cudaMemcpyAsync(&h, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  if (h & kErrTimeout) {
+    cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
+    return fail(DC_GB300_ERR_TIMEOUT, "a TMA wait in the stencil kernel timed out");
+  }
+  return DC_GB300_OK;
+}
+
+bool env_is(const char *name, const char *value) {
+  const char *v = std::getenv(name);
+  return v && std::strcmp(v, value) == 0;
+}
+
+[[noreturn]] void abi_die(const char *where) {
+  std::fprintf(stderr, "[dc_gb300] %s: %s\n", where, g_err.c_str());
+  std::exit(1);
+}
+
+}  // namespace
+}  // namespace dcg
+
+using namespace dcg;
+
+// ===========================================================================
+// dc_gb300_* API
+// ===========================================================================
+
+extern "C" const char *dc_gb300_last_error(void) { return g_err.c_str(); }
+
+extern "C" const char *dc_gb300_version(void) { return "dc_gb300 1.0 (sm_103a)"; }
+
+extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
+  if (!cfg || !out) return fail(DC_GB300_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (cfg->sx < 9 || cfg->sy < 9 || cfg->sz < 9)
+    return fail(DC_GB300_ERR_ARG, "every size must be >= 9 (4-cell halo on both sides)");
+  if (cfg->sx > (1 << 30) || cfg->sy > (1 << 30) || cfg->sz > (1 << 30))
+    return fail(DC_GB300_ERR_ARG, "size too large");
+  if (cfg->kernel != DC_GB300_KERNEL_FAST && cfg->kernel != DC_GB300_KERNEL_EXACT)
+    return fail(DC_GB300_ERR_ARG, "unknown kernel");
+  if (cfg->medium != DC_GB300_MEDIUM_PRECOMP && cfg->medium != DC_GB300_MEDIUM_VPZ_VSV)
+    return fail(DC_GB300_ERR_ARG, "unknown medium form");
+  if (!(cfg->dx > 0 && cfg->dy > 0 && cfg->dz > 0 && cfg->dt > 0))
+    return fail(DC_GB300_ERR_ARG, "dx, dy, dz and dt must be positive");
+  int dev = cfg->device;
+  if (dev < 0) DCG_TRY(cudaGetDevice(&dev));
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(DC_GB300_ERR_DEVICE, "no CUDA device");
+  if (dev >= ndev) return fail(DC_GB300_ERR_DEVICE, "device ordinal out of range");
+  cudaDeviceProp prop;
+  DCG_TRY(cudaGetDeviceProperties(&prop, dev));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(DC_GB300_ERR_DEVICE,
+                std::string("this build targets sm_103a; device is ") + prop.name);
+  DCG_TRY(cudaSetDevice(dev));
+
+  auto *h = new dc_gb300_sim();
+  auto *s = new Sim();
+  h->impl = s;
+  s->handle = h;
+  s->device = dev;
+  s->sx = cfg->sx;
+  s->sy = cfg->sy;
+  s->sz = cfg->sz;
+  s->pitch = round_up4(cfg->sx);
+  s->plane = s->pitch * s->sy;
+  s->count = s->plane * s->sz;
+  s->dx = cfg->dx;
+  s->dy = cfg->dy;
+  s->dz = cfg->dz;
+  s->dt = cfg->dt;
+  s->kernel = cfg->kernel;
+  s->medium = cfg->medium;
+  auto bail = [&](int code) {
+    release(s);
+    delete s;
+    delete h;
+    return code;
+  };
+  // Blocking stream: the legacy default stream orders with it, so callers'
+  // own cudaMemcpy on data->pc etc. see the finished results.
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamDefault) != cudaSuccess)
+    return bail(fail(DC_GB300_ERR_CUDA, "cudaStreamCreate failed"));
+  const size_t bytes = static_cast<size_t>(s->count) * 4;
+  for (int b = 0; b < 4; ++b)
+    if (cudaMalloc(&s->field[b], bytes) != cudaSuccess)
+      return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of a wavefield failed"));
+  if (s->medium == DC_GB300_MEDIUM_PRECOMP) {
+    if (cudaMalloc(&s->coef, bytes * DC_NCOEF) != cudaSuccess)
+      return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of the coefficients failed"));
+  } else {
+    if (cudaMalloc(&s->vv, bytes * 2) != cudaSuccess)
+      return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of vpz/vsv failed"));
+  }
+  if (cudaMalloc(&s->d_step, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->d_src_pre, 2 * sizeof(float)) != cudaSuccess)
+    return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of counters failed"));
+  for (int b = 0; b < 4; ++b)
+    if (cudaMemsetAsync(s->field[b], 0, bytes, s->stream) != cudaSuccess)
+      return bail(fail(DC_GB300_ERR_CUDA, "cudaMemset failed"));
+  if (s->coef) cudaMemsetAsync(s->coef, 0, bytes * DC_NCOEF, s->stream);
+  if (s->vv) cudaMemsetAsync(s->vv, 0, bytes * 2, s->stream);
+  cudaMemsetAsync(s->d_step, 0, sizeof(int), s->stream);
+  cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
+  cudaMemsetAsync(s->d_src_pre, 0, 2 * sizeof(float), s->stream);
+  std::string err;
+  if (s->kernel == DC_GB300_KERNEL_FAST && !fast_encode_maps(s, &err))
+    return bail(fail(DC_GB300_ERR_CUDA, err));
+  h->abi.pp = s->field[0];
+  h->abi.pc = s->field[1];
+  h->abi.qp = s->field[2];
+  h->abi.qc = s->field[3];
+  refresh_abi(s);
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess)
+    return bail(fail(DC_GB300_ERR_CUDA, "initialisation failed"));
+  *out = h;
+  return DC_GB300_OK;
+}
+
+extern "C" void dc_gb300_destroy(dc_gb300_sim *h) {
+  if (!h) return;
+  Sim *s = h->impl;
+  if (s) {
+    cudaSetDevice(s->device);
+    release(s);
+    delete s;
+  }
+  delete h;
+}
+
+extern "C" dc_device_data *dc_gb300_device_data(dc_gb300_sim *h) {
+  return h ? &h->abi : nullptr;
+}
+
+extern "C" dc_gb300_sim *dc_gb300_from_device_data(dc_device_data *d) {
+  return reinterpret_cast<dc_gb300_sim *>(d);
+}
+
+extern "C" long dc_gb300_device_pitch(const dc_gb300_sim *h) {
+  return h && h->impl ? static_cast<long>(h->impl->pitch) : 0;
+}
+
+extern "C" void *dc_gb300_stream(dc_gb300_sim *h) {
+  return h && h->impl ? static_cast<void *>(h->impl->stream) : nullptr;
+}
+
+extern "C" long dc_gb300_kernel_launches(const dc_gb300_sim *h) {
+  return h && h->impl ? static_cast<long>(h->impl->launches) : 0;
+}
+
+extern "C" long dc_gb300_steps_done(const dc_gb300_sim *h) {
+  return h && h->impl ? static_cast<long>(h->impl->steps_done) : 0;
+}
+
+extern "C" int dc_gb300_set_precomp(dc_gb300_sim *h, const dc_precomp_vars *host) {
+  Sim *s = impl(h);
+  if (!s || !host) return fail(DC_GB300_ERR_ARG, "null argument");
+  if (!s->coef) return fail(DC_GB300_ERR_STATE, "simulation uses the vpz/vsv medium form");
+  const float *src[10] = {host->ch1dxx, host->ch1dyy, host->ch1dzz, host->ch1dxy,
+                          host->ch1dyz, host->ch1dxz, host->v2px,   host->v2pz,
+                          host->v2sz,   host->v2pn};
+  DCG_TRY(cudaSetDevice(s->device));
+  for (int k = 0; k < 10; ++k) {
+    if (!src[k]) return fail(DC_GB300_ERR_ARG, "a coefficient array is null");
+    DCG_TRY(upload_dense(s, s->coef + kRefToDev[k] * s->count, src[k]));
+  }
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_set_vpz_vsv(dc_gb300_sim *h, const float *vpz, const float *vsv) {
+  Sim *s = impl(h);
+  if (!s || !vpz || !vsv) return fail(DC_GB300_ERR_ARG, "null argument");
+  if (!s->vv) return fail(DC_GB300_ERR_STATE, "simulation uses the ten-coefficient medium form");
+  DCG_TRY(cudaSetDevice(s->device));
+  DCG_TRY(upload_dense(s, s->vv, vpz));
+  DCG_TRY(upload_dense(s, s->vv + s->count, vsv));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_get_precomp(dc_gb300_sim *h, const dc_precomp_vars *host) {
+  Sim *s = impl(h);
+  if (!s || !host) return fail(DC_GB300_ERR_ARG, "null argument");
+  if (!s->coef) return fail(DC_GB300_ERR_STATE, "simulation uses the vpz/vsv medium form");
+  float *dst[10] = {host->ch1dxx, host->ch1dyy, host->ch1dzz, host->ch1dxy, host->ch1dyz,
+                    host->ch1dxz, host->v2px,   host->v2pz,   host->v2sz,   host->v2pn};
+  DCG_TRY(cudaSetDevice(s->device));
+  for (int k = 0; k < 10; ++k)
+    if (dst[k]) DCG_TRY(download_dense(s, dst[k], s->coef + kRefToDev[k] * s->count));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_get_vpz_vsv(dc_gb300_sim *h, float *vpz, float *vsv) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null argument");
+  if (!s->vv) return fail(DC_GB300_ERR_STATE, "simulation uses the ten-coefficient medium form");
+  DCG_TRY(cudaSetDevice(s->device));
+  if (vpz) DCG_TRY(download_dense(s, vpz, s->vv));
+  if (vsv) DCG_TRY(download_dense(s, vsv, s->vv + s->count));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+namespace {
+// GPU FP64 precompute from dense host anisotropy arrays into `coef_dense`
+// (10 dense arrays of n floats, device order).
+int precompute_dense(cudaStream_t st, const dc_anisotropy_t *a, long long n,
+                     float *coef_dense) {
+  const float *src[6] = {a->theta, a->phi, a->vsv, a->vpz, a->epsilon, a->delta};
+  for (const float *p : src)
+    if (!p) return fail(DC_GB300_ERR_ARG, "an anisotropy array is null");
+  float *d_in = nullptr;
+  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&d_in), sizeof(float) * n * 6, st));
+  for (int k = 0; k < 6; ++k)
+    DCG_TRY(cudaMemcpyAsync(d_in + k * n, src[k], sizeof(float) * n,
+                            cudaMemcpyHostToDevice, st));
+  DCG_TRY(launch_precomp(st, d_in, d_in + n, d_in + 2 * n, d_in + 3 * n, d_in + 4 * n,
+                         d_in + 5 * n, coef_dense, n, n));
+  DCG_TRY(cudaFreeAsync(d_in, st));
+  return DC_GB300_OK;
+}
+}  // namespace
+
+extern "C" int dc_gb300_set_anisotropy(dc_gb300_sim *h, const dc_anisotropy_t *host) {
+  Sim *s = impl(h);
+  if (!s || !host) return fail(DC_GB300_ERR_ARG, "null argument");
+  DCG_TRY(cudaSetDevice(s->device));
+  const long long n = s->sx * s->sy * s->sz;
+  if (s->vv) {
+    if (!host->vpz || !host->vsv) return fail(DC_GB300_ERR_ARG, "vpz/vsv null");
+    DCG_TRY(upload_dense(s, s->vv, host->vpz));
+    DCG_TRY(upload_dense(s, s->vv + s->count, host->vsv));
+  }
+  if (s->coef) {
+    float *dense = nullptr;
+    DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&dense), sizeof(float) * n * DC_NCOEF,
+                            s->stream));
+    int rc = precompute_dense(s->stream, host, n, dense);
+    if (rc != DC_GB300_OK) return rc;
+    for (int k = 0; k < DC_NCOEF; ++k)
+      DCG_TRY(cudaMemcpy2DAsync(s->coef + k * s->count, s->pitch * 4, dense + k * n,
+                                s->sx * 4, s->sx * 4, s->sy * s->sz,
+                                cudaMemcpyDeviceToDevice, s->stream));
+    DCG_TRY(cudaFreeAsync(dense, s->stream));
+  }
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_generate_layered(dc_gb300_sim *h, const dc_gb300_layered_spec *spec) {
+  Sim *s = impl(h);
+  if (!s || !spec) return fail(DC_GB300_ERR_ARG, "null argument");
+  if (spec->nlayers < 1 || spec->nlayers > DC_GB300_MAX_LAYERS ||
+      spec->n_noise < 0 || spec->n_noise > DC_GB300_MAX_FEATURES ||
+      spec->n_theta < 0 || spec->n_theta > DC_GB300_MAX_FEATURES ||
+      spec->n_phi < 0 || spec->n_phi > DC_GB300_MAX_FEATURES || !(spec->sigma_ratio > 0))
+    return fail(DC_GB300_ERR_ARG, "invalid layered-medium spec");
+  DCG_TRY(cudaSetDevice(s->device));
+  ++s->launches;
+  DCG_TRY(launch_layered(s->stream, *spec, s->coef, s->vv, s->sx, s->sy, s->sz, s->pitch,
+                         s->count));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_set_fields(dc_gb300_sim *h, const float *pp, const float *pc,
+                                   const float *qp, const float *qc) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
+  DCG_TRY(cudaSetDevice(s->device));
+  dc_device_data &a = h->abi;
+  float *dst[4] = {a.pp, a.pc, a.qp, a.qc};
+  const float *src[4] = {pp, pc, qp, qc};
+  for (int k = 0; k < 4; ++k) {
+    if (src[k]) {
+      DCG_TRY(upload_dense(s, dst[k], src[k]));
+    } else {
+      DCG_TRY(cudaMemsetAsync(dst[k], 0, static_cast<size_t>(s->count) * 4, s->stream));
+    }
+  }
+  DCG_TRY(cudaMemsetAsync(s->d_step, 0, sizeof(int), s->stream));
+  if (s->d_energy) DCG_TRY(cudaMemsetAsync(s->d_energy, 0, sizeof(double) * s->energy_cap, s->stream));
+  if (s->d_traces)
+    DCG_TRY(cudaMemsetAsync(s->d_traces, 0, sizeof(float) * s->trace_cap * s->nrec, s->stream));
+  s->steps_done = 0;
+  s->src_applied_step = -1;
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_get_fields(dc_gb300_sim *h, float *pp, float *pc, float *qp,
+                                   float *qc) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
+  DCG_TRY(cudaSetDevice(s->device));
+  dc_device_data &a = h->abi;
+  float *dst[4] = {pp, pc, qp, qc};
+  const float *src[4] = {a.pp, a.pc, a.qp, a.qc};
+  for (int k = 0; k < 4; ++k)
+    if (dst[k]) DCG_TRY(download_dense(s, dst[k], src[k]));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_set_source(dc_gb300_sim *h, long index, const float *amp, int count) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
+  DCG_TRY(cudaSetDevice(s->device));
+  drop_graphs(s);
+  ++s->config_version;
+  if (index < 0) {
+    s->src_gi = -1;
+    s->src_x = s->src_y = s->src_z = -1;
+    return DC_GB300_OK;
+  }
+  const long long n = s->sx * s->sy * s->sz;
+  if (index >= n || count < 0 || (count > 0 && !amp))
+    return fail(DC_GB300_ERR_ARG, "source index or amplitudes invalid");
+  const long long x = index % s->sx, y = (index / s->sx) % s->sy, z = index / (s->sx * s->sy);
+  if (x < 4 || x >= s->sx - 4 || y < 4 || y >= s->sy - 4 || z < 4 || z >= s->sz - 4)
+    return fail(DC_GB300_ERR_ARG, "the source must lie in the updated region [4, s-4)^3");
+  if (count > s->src_count || !s->d_src) {
+    cudaFree(s->d_src);
+    s->d_src = nullptr;
+    DCG_TRY(cudaMalloc(&s->d_src, sizeof(float) * std::max(count, 1)));
+  }
+  if (count > 0)
+    DCG_TRY(cudaMemcpyAsync(s->d_src, amp, sizeof(float) * count, cudaMemcpyHostToDevice,
+                            s->stream));
+  s->src_count = count;
+  s->src_x = static_cast<int>(x);
+  s->src_y = static_cast<int>(y);
+  s->src_z = static_cast<int>(z);
+  s->src_gi = z * s->plane + y * s->pitch + x;
+  s->src_applied_step = -1;
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_set_sponge(dc_gb300_sim *h, const float *gx, const float *gy,
+                                   const float *gz) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
+  DCG_TRY(cudaSetDevice(s->device));
+  drop_graphs(s);
+  ++s->config_version;
+  if (!gx || !gy || !gz) {
+    s->has_sponge = false;
+    return DC_GB300_OK;
+  }
+  if (!s->sponge)
+    DCG_TRY(cudaMalloc(&s->sponge, sizeof(float) * (s->sx + s->sy + s->sz)));
+  DCG_TRY(cudaMemcpyAsync(s->sponge, gx, sizeof(float) * s->sx, cudaMemcpyHostToDevice, s->stream));
+  DCG_TRY(cudaMemcpyAsync(s->sponge + s->sx, gy, sizeof(float) * s->sy, cudaMemcpyHostToDevice,
+                          s->stream));
+  DCG_TRY(cudaMemcpyAsync(s->sponge + s->sx + s->sy, gz, sizeof(float) * s->sz,
+                          cudaMemcpyHostToDevice, s->stream));
+  s->has_sponge = true;
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_set_receivers(dc_gb300_sim *h, const long *index, int count,
+                                      int max_steps) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
+  DCG_TRY(cudaSetDevice(s->device));
+  drop_graphs(s);
+  ++s->config_version;
+  cudaFree(s->d_rec);
+  cudaFree(s->d_traces);
+  s->d_rec = nullptr;
+  s->d_traces = nullptr;
+  s->nrec = 0;
+  s->trace_cap = 0;
+  if (count <= 0) return DC_GB300_OK;
+  if (!index || max_steps <= 0) return fail(DC_GB300_ERR_ARG, "receivers invalid");
+  const long long n = s->sx * s->sy * s->sz;
+  std::vector<long long> pidx(count);
+  for (int r = 0; r < count; ++r) {
+    if (index[r] < 0 || index[r] >= n) return fail(DC_GB300_ERR_ARG, "receiver index out of range");
+    const long long i = index[r];
+    const long long x = i % s->sx, y = (i / s->sx) % s->sy, z = i / (s->sx * s->sy);
+    pidx[r] = z * s->plane + y * s->pitch + x;
+  }
+  DCG_TRY(cudaMalloc(&s->d_rec, sizeof(long long) * count));
+  DCG_TRY(cudaMalloc(&s->d_traces, sizeof(float) * static_cast<size_t>(count) * max_steps));
+  DCG_TRY(cudaMemcpyAsync(s->d_rec, pidx.data(), sizeof(long long) * count,
+                          cudaMemcpyHostToDevice, s->stream));
+  DCG_TRY(cudaMemsetAsync(s->d_traces, 0, sizeof(float) * static_cast<size_t>(count) * max_steps,
+                          s->stream));
+  s->nrec = count;
+  s->trace_cap = max_steps;
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_get_traces(dc_gb300_sim *h, float *out, int steps) {
+  Sim *s = impl(h);
+  if (!s || !out) return fail(DC_GB300_ERR_ARG, "null argument");
+  if (steps < 0 || steps > s->trace_cap) return fail(DC_GB300_ERR_ARG, "steps beyond capacity");
+  DCG_TRY(cudaSetDevice(s->device));
+  DCG_TRY(cudaMemcpyAsync(out, s->d_traces, sizeof(float) * static_cast<size_t>(steps) * s->nrec,
+                          cudaMemcpyDeviceToHost, s->stream));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_enable_energy(dc_gb300_sim *h, int max_steps) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
+  DCG_TRY(cudaSetDevice(s->device));
+  drop_graphs(s);
+  ++s->config_version;
+  cudaFree(s->d_energy);
+  s->d_energy = nullptr;
+  s->energy_cap = 0;
+  if (max_steps <= 0) return DC_GB300_OK;
+  DCG_TRY(cudaMalloc(&s->d_energy, sizeof(double) * max_steps));
+  DCG_TRY(cudaMemsetAsync(s->d_energy, 0, sizeof(double) * max_steps, s->stream));
+  s->energy_cap = max_steps;
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_get_energy(dc_gb300_sim *h, double *out, int steps) {
+  Sim *s = impl(h);
+  if (!s || !out) return fail(DC_GB300_ERR_ARG, "null argument");
+  if (steps < 0 || steps > s->energy_cap) return fail(DC_GB300_ERR_ARG, "steps beyond capacity");
+  DCG_TRY(cudaSetDevice(s->device));
+  DCG_TRY(cudaMemcpyAsync(out, s->d_energy, sizeof(double) * steps, cudaMemcpyDeviceToHost,
+                          s->stream));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+namespace {
+
+// Captures kGraphChunk steps (+ the step-counter advance) into a graph.
+int capture_chunk(Sim *s, cudaGraphExec_t *out) {
+  cudaGraph_t g = nullptr;
+  DCG_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  const dc_device_data saved = s->handle->abi;
+  const long long saved_launches = s->launches;
+  cudaError_t e = cudaSuccess;
+  for (int j = 0; j < kGraphChunk && e == cudaSuccess; ++j) e = queue_step(s, j);
+  if (e == cudaSuccess) e = launch_advance_step(s->stream, s->d_step, kGraphChunk);
+  cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+  // capture only recorded the work: restore the roles and counters
+  s->handle->abi = saved;
+  s->launches = saved_launches;
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(DC_GB300_ERR_CUDA, std::string("graph capture failed: ") +
+                                       cudaGetErrorString(e != cudaSuccess ? e : e2));
+  }
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess)
+    return fail(DC_GB300_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  return DC_GB300_OK;
+}
+
+long long launches_per_step(const Sim *s) { return 1 + (s->nrec > 0 ? 1 : 0); }
+
+}  // namespace
+
+extern "C" int dc_gb300_run(dc_gb300_sim *h, int steps) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
+  if (steps < 0) return fail(DC_GB300_ERR_ARG, "negative step count");
+  if (steps == 0) return DC_GB300_OK;
+  DCG_TRY(cudaSetDevice(s->device));
+  if (s->energy_cap > 0 && s->steps_done + steps > s->energy_cap)
+    return fail(DC_GB300_ERR_ARG, "run exceeds the energy capacity");
+  if (s->nrec > 0 && s->steps_done + steps > s->trace_cap)
+    return fail(DC_GB300_ERR_ARG, "run exceeds the trace capacity");
+  // The source of the first step of this run goes in before the stencil
+  // (src/worker.c:467-470); later ones are fused into the previous store.
+  if (s->src_gi >= 0 && s->src_applied_step != s->steps_done) {
+    ++s->launches;
+    DCG_TRY(launch_add_source(s->stream, h->abi.pc, h->abi.qc, s->src_gi, s->d_src,
+                              s->src_count, s->d_step, 0));
+  }
+  int left = steps;
+  while (left >= kGraphChunk) {
+    const int par = buffer_of(s, h->abi.pc) & 1;  // pc is buffer 1 or 0
+    const int slot = par;
+    if (!s->graph[slot] || s->graph_version[slot] != s->config_version ||
+        s->graph_pc[slot] != buffer_of(s, h->abi.pc)) {
+      if (s->graph[slot]) cudaGraphExecDestroy(s->graph[slot]);
+      s->graph[slot] = nullptr;
+      int rc = capture_chunk(s, &s->graph[slot]);
+      if (rc != DC_GB300_OK) return rc;
+      s->graph_version[slot] = s->config_version;
+      s->graph_pc[slot] = buffer_of(s, h->abi.pc);
+    }
+    DCG_TRY(cudaGraphLaunch(s->graph[slot], s->stream));
+    s->launches += kGraphChunk * launches_per_step(s) + 1;
+    // kGraphChunk is even: the roles are back where they started
+    left -= kGraphChunk;
+    s->steps_done += kGraphChunk;
+  }
+  for (int j = 0; j < left; ++j) DCG_TRY(queue_step(s, j));
+  if (left > 0) {
+    ++s->launches;
+    DCG_TRY(launch_advance_step(s->stream, s->d_step, left));
+    s->steps_done += left;
+  }
+  if (s->src_gi >= 0) s->src_applied_step = s->steps_done;
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_synchronize(dc_gb300_sim *h) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
+  DCG_TRY(cudaSetDevice(s->device));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return check_err_word(s);
+}
+
+extern "C" int dc_gb300_propagate_box(dc_gb300_sim *h, const size_t start[3],
+                                      const size_t end[3]) {
+  Sim *s = impl(h);
+  if (!s || !start || !end) return fail(DC_GB300_ERR_ARG, "null argument");
+  const long long lim[3] = {s->sx, s->sy, s->sz};
+  long long b0[3], b1[3];
+  for (int d = 0; d < 3; ++d) {
+    if (end[d] <= start[d]) return DC_GB300_OK;  // empty box: nothing to do
+    b0[d] = static_cast<long long>(start[d]);
+    b1[d] = static_cast<long long>(end[d]);
+    if (b0[d] < 4 || b1[d] > lim[d] - 4)
+      return fail(DC_GB300_ERR_ARG, "box outside the updatable region [4, size-4)");
+  }
+  const dc_device_data &a = h->abi;
+  if (buffer_of(s, a.pp) < 0 || buffer_of(s, a.pc) < 0 || buffer_of(s, a.qp) < 0 ||
+      buffer_of(s, a.qc) < 0)
+    return fail(DC_GB300_ERR_STATE, "field pointers do not belong to this simulation");
+  DCG_TRY(cudaSetDevice(s->device));
+  StepParams p = make_params(s, b0, b1, s->dx, s->dy, s->dz, s->dt);
+  DCG_TRY(launch_pass(s, p));
+  return DC_GB300_OK;
+}
+
+// ===========================================================================
+// The reference's device-data and propagate entry points
+// (include/device_data.h, include/propagate.h)
+// ===========================================================================
+
+extern "C" dc_device_data *dc_device_data_init(dc_process_t *process) {
+  if (!process) {
+    set_error("null process");
+    abi_die("dc_device_data_init");
+  }
+  dc_gb300_config cfg{};
+  cfg.sx = static_cast<long>(process->sizes[0]);
+  cfg.sy = static_cast<long>(process->sizes[1]);
+  cfg.sz = static_cast<long>(process->sizes[2]);
+  cfg.dx = process->dx;
+  cfg.dy = process->dy;
+  cfg.dz = process->dz;
+  cfg.dt = process->dt;
+  cfg.kernel = env_is("DC_GB300_KERNEL", "exact") ? DC_GB300_KERNEL_EXACT : DC_GB300_KERNEL_FAST;
+  cfg.medium = env_is("DC_GB300_MEDIUM", "vpz_vsv") ? DC_GB300_MEDIUM_VPZ_VSV
+                                                    : DC_GB300_MEDIUM_PRECOMP;
+  const char *dev = std::getenv("DC_GB300_DEVICE");
+  cfg.device = dev ? std::atoi(dev) : 0;
+  // dt etc. may be left 0 by callers that pass them to dc_propagate only
+  if (!(cfg.dx > 0)) cfg.dx = 1;
+  if (!(cfg.dy > 0)) cfg.dy = 1;
+  if (!(cfg.dz > 0)) cfg.dz = 1;
+  if (!(cfg.dt > 0)) cfg.dt = 1;
+  dc_gb300_sim *h = nullptr;
+  if (dc_gb300_create(&cfg, &h) != DC_GB300_OK) abi_die("dc_device_data_init");
+  int rc = DC_GB300_OK;
+  if (cfg.medium == DC_GB300_MEDIUM_PRECOMP) {
+    if (process->precomp_vars.ch1dxx)
+      rc = dc_gb300_set_precomp(h, &process->precomp_vars);
+    else
+      rc = dc_gb300_set_anisotropy(h, &process->anisotropy_vars);
+  } else {
+    rc = dc_gb300_set_vpz_vsv(h, process->anisotropy_vars.vpz, process->anisotropy_vars.vsv);
+  }
+  if (rc == DC_GB300_OK)
+    rc = dc_gb300_set_fields(h, process->pp, process->pc, process->qp, process->qc);
+  if (rc != DC_GB300_OK) {
+    const std::string msg = g_err;
+    dc_gb300_destroy(h);
+    set_error(msg);
+    abi_die("dc_device_data_init");
+  }
+  return &h->abi;
+}
+
+extern "C" void dc_device_data_free(dc_device_data *data) {
+  dc_gb300_destroy(dc_gb300_from_device_data(data));
+}
+
+extern "C" void dc_device_data_get_results(dc_process_t *process, dc_device_data *data) {
+  dc_gb300_sim *h = dc_gb300_from_device_data(data);
+  if (!process || !h) {
+    set_error("null argument");
+    abi_die("dc_device_data_get_results");
+  }
+  if (dc_gb300_synchronize(h) != DC_GB300_OK ||
+      dc_gb300_get_fields(h, nullptr, process->pc, nullptr, process->qc) != DC_GB300_OK)
+    abi_die("dc_device_data_get_results");
+}
+
+extern "C" void dc_device_swap_arrays(dc_device_data *data) {
+  // src/device_data.cu:119-129
+  std::swap(data->pp, data->pc);
+  std::swap(data->qp, data->qc);
+}
+
+extern "C" void dc_device_add_source(dc_device_data *data, size_t index, float source) {
+  dc_gb300_sim *h = dc_gb300_from_device_data(data);
+  Sim *s = impl(h);
+  const long long n = s->sx * s->sy * s->sz;
+  if (static_cast<long long>(index) >= n) {
+    set_error("source index out of range");
+    abi_die("dc_device_add_source");
+  }
+  const long long i = static_cast<long long>(index);
+  const long long x = i % s->sx, y = (i / s->sx) % s->sy, z = i / (s->sx * s->sy);
+  ++s->launches;
+  cudaError_t e = launch_add_value(s->stream, data->pc, data->qc,
+                                   z * s->plane + y * s->pitch + x, source);
+  if (e != cudaSuccess) {
+    set_error(cudaGetErrorString(e));
+    abi_die("dc_device_add_source");
+  }
+}
+
+extern "C" void dc_propagate(const size_t start_coords[3], const size_t end_coords[3],
+                             const size_t sizes[3], const int *, const int *,
+                             dc_device_data *data, const float dx, const float dy,
+                             const float dz, const float dt) {
+  dc_gb300_sim *h = dc_gb300_from_device_data(data);
+  Sim *s = impl(h);
+  if (!s || !sizes || static_cast<long long>(sizes[0]) != s->sx ||
+      static_cast<long long>(sizes[1]) != s->sy || static_cast<long long>(sizes[2]) != s->sz) {
+    set_error("sizes differ from the ones given to dc_device_data_init");
+    abi_die("dc_propagate");
+  }
+  // the step sizes come with every call, as in the reference
+  s->dx = dx;
+  s->dy = dy;
+  s->dz = dz;
+  s->dt = dt;
+  if (dc_gb300_propagate_box(h, start_coords, end_coords) != DC_GB300_OK)
+    abi_die("dc_propagate");
+}
+
+namespace {
+void halo_copy(dc_device_data *data, float *host, const size_t start[3], const size_t end[3],
+               const size_t sizes[3], float *dev, bool to_host, const char *where) {
+  Sim *s = impl(dc_gb300_from_device_data(data));
+  if (!s || !host || !dev || !start || !end || !sizes) {
+    set_error("null argument");
+    abi_die(where);
+  }
+  for (int d = 0; d < 3; ++d)
+    if (end[d] < start[d] || end[d] > sizes[d]) {
+      set_error("box outside the array");
+      abi_die(where);
+    }
+  const size_t w = end[0] - start[0], hgt = end[1] - start[1], dep = end[2] - start[2];
+  if (w == 0 || hgt == 0 || dep == 0) return;
+  cudaMemcpy3DParms p{};
+  cudaPitchedPtr devp = make_cudaPitchedPtr(dev, s->pitch * 4, s->sx, s->sy);
+  cudaPitchedPtr hostp = make_cudaPitchedPtr(host, w * 4, w, hgt);
+  cudaPos devpos = make_cudaPos(start[0] * 4, start[1], start[2]);
+  if (to_host) {
+    p.srcPtr = devp;
+    p.srcPos = devpos;
+    p.dstPtr = hostp;
+    p.kind = cudaMemcpyDeviceToHost;
+  } else {
+    p.srcPtr = hostp;
+    p.dstPtr = devp;
+    p.dstPos = devpos;
+    p.kind = cudaMemcpyHostToDevice;
+  }
+  p.extent = make_cudaExtent(w * 4, hgt, dep);
+  cudaError_t e = cudaMemcpy3DAsync(&p, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) {
+    set_error(cudaGetErrorString(e));
+    abi_die(where);
+  }
+}
+}  // namespace
+
+extern "C" void dc_device_extract_halo_face(dc_device_data *data, float *buffer,
+                                            const size_t start_coords[3],
+                                            const size_t end_coords[3], const size_t sizes[3],
+                                            const float *from_array) {
+  halo_copy(data, buffer, start_coords, end_coords, sizes, const_cast<float *>(from_array), true,
+            "dc_device_extract_halo_face");
+}
+
+extern "C" void dc_device_insert_halo_face(dc_device_data *data, const float *buffer,
+                                           const size_t start_coords[3],
+                                           const size_t end_coords[3], const size_t sizes[3],
+                                           float *to_array) {
+  halo_copy(data, const_cast<float *>(buffer), start_coords, end_coords, sizes, to_array, false,
+            "dc_device_insert_halo_face");
+}
+
+// dc_compute_precomp_vars on the GPU (FP64 trig), returned as host arrays.
+extern "C" dc_precomp_vars dc_compute_precomp_vars(int sx, int sy, int sz,
+                                                   dc_anisotropy_t anisotropy) {
+  dc_precomp_vars v{};
+  const long long n = static_cast<long long>(sx) * sy * sz;
+  float **dst[10] = {&v.ch1dxx, &v.ch1dyy, &v.ch1dzz, &v.ch1dxy, &v.ch1dyz,
+                     &v.ch1dxz, &v.v2px,   &v.v2pz,   &v.v2sz,   &v.v2pn};
+  for (float **d : dst) {
+    *d = static_cast<float *>(std::malloc(sizeof(float) * std::max<long long>(n, 1)));
+    if (!*d) {
+      set_error("OOM in dc_compute_precomp_vars");
+      abi_die("dc_compute_precomp_vars");
+    }
+  }
+  if (n == 0) return v;
+  cudaStream_t st = nullptr;
+  float *dense = nullptr;
+  if (cudaStreamCreate(&st) != cudaSuccess ||
+      cudaMallocAsync(reinterpret_cast<void **>(&dense), sizeof(float) * n * DC_NCOEF, st) !=
+          cudaSuccess) {
+    set_error("CUDA set-up failed in dc_compute_precomp_vars");
+    abi_die("dc_compute_precomp_vars");
+  }
+  if (precompute_dense(st, &anisotropy, n, dense) != DC_GB300_OK) abi_die("dc_compute_precomp_vars");
+  for (int k = 0; k < 10; ++k)
+    if (cudaMemcpyAsync(*dst[k], dense + kRefToDev[k] * n, sizeof(float) * n,
+                        cudaMemcpyDeviceToHost, st) != cudaSuccess) {
+      set_error("copy-back failed in dc_compute_precomp_vars");
+      abi_die("dc_compute_precomp_vars");
+    }
+  cudaFreeAsync(dense, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) {
+    set_error("dc_compute_precomp_vars kernel failed");
+    abi_die("dc_compute_precomp_vars");
+  }
+  cudaStreamDestroy(st);
+  return v;
+}

@@ -1,0 +1,486 @@
+// tti_fast.cu -- the fast sm_103a Fletcher TTI time step.
+//
+// One pass updates p and q (the coupled pseudo-acoustic TTI system of the
+// reference, include/sample_compute.h:105-185) for every point of a box.
+//
+// Work decomposition: a CTA owns a TX x TY column tile in (x, y) and sweeps
+// a chunk of output planes along z.  For the leading plane k it receives,
+// by TMA into a NSTAGE-deep shared-memory ring:
+//   * the p and q planes k with a 4-cell halo in x and y,
+//   * cxx, cyy, cxy at plane k   (in-plane coefficients),
+//   * the other seven coefficients and pp, qp at the output plane z = k - 4.
+// Each thread owns one (x, y) column and keeps, in registers, a 9-deep queue
+// per field of the centre value, the unscaled first x-derivative and the
+// unscaled first y-derivative.  The cross derivatives are evaluated in their
+// separable form: with the 8th-order first-derivative weights L1..L4, the
+// reference's 64-point derCross (include/derivatives.h:56-91) equals
+// D_a(D_b p) because its weights are L_ab = L_a * L_b.  So
+//   d2p/dxdy  = D_x of the y-derivative plane (shared memory, per plane),
+//   d2p/dxdz  = D_z of the x-derivative queue (registers),
+//   d2p/dydz  = D_z of the y-derivative queue (registers),
+// and the in-plane part of H1/H2 is formed at the leading plane and delayed
+// four planes in registers.  Rounding differs from the reference's direct
+// sums (see the exact kernel for bit-identical results).
+//
+// Algorithmic (compulsory) DRAM traffic per point-update: read pc, qc, pp,
+// qp and ten coefficients, write pp and qp: 64 bytes (32 bytes for the
+// vpz/vsv medium form).
+#include <cstdio>
+
+#include "dc_internal.h"
+#include "dc_ptx.cuh"
+
+namespace dcg {
+namespace {
+
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per TMA wait
+
+constexpr int align128(int b) { return (b + 127) / 128 * 128; }
+
+template <int TX, int TY, int NSTAGE, int MEDIUM>
+struct FastLayout {
+  static constexpr int HX = TX + 2 * kHalo;
+  static constexpr int HY = TY + 2 * kHalo;
+  static constexpr int NT = TX * TY;
+  static constexpr int NCA = MEDIUM == DC_GB300_MEDIUM_PRECOMP ? 3 : 0;
+  static constexpr int NCB = MEDIUM == DC_GB300_MEDIUM_PRECOMP ? 7 : 2;
+  static constexpr int HALO_BYTES = align128(HX * HY * 4);
+  static constexpr int TILE_BYTES = NT * 4;  // NT % 32 == 0: 128-B multiple
+  static constexpr int OFF_HP = 0;
+  static constexpr int OFF_HQ = HALO_BYTES;
+  static constexpr int OFF_CA = 2 * HALO_BYTES;
+  static constexpr int OFF_CB = OFF_CA + NCA * TILE_BYTES;
+  static constexpr int OFF_OWN = OFF_CB + NCB * TILE_BYTES;
+  static constexpr int STAGE_BYTES = OFF_OWN + 2 * TILE_BYTES;
+  static constexpr int DY_BYTES = align128(TY * HX * 4);
+  static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;  // [parity][field]
+  static constexpr int OFF_BAR = OFF_DY + 4 * DY_BYTES;
+  static constexpr int SMEM_BYTES = OFF_BAR + NSTAGE * 8 + 128;
+  static constexpr uint32_t TX_HALO = 2u * HX * HY * 4u;
+  static constexpr uint32_t TX_CA = NCA * NT * 4u;
+  static constexpr uint32_t TX_OUT = (NCB + 2) * NT * 4u;
+  static_assert(TX % 32 == 0, "a warp spans one tile row");
+  static_assert(HX * 4 % 16 == 0, "TMA box rows are 16-byte multiples");
+  static_assert(8 * TY <= NT, "halo-column work fits the CTA");
+};
+
+// 8th-order second derivative (unscaled), weights K0..K4.
+__device__ __forceinline__ float d2w(float c, float m1, float p1, float m2,
+                                     float p2, float m3, float p3, float m4,
+                                     float p4) {
+  float a = DCG_K0 * c;
+  a = fmaf(DCG_K1, m1 + p1, a);
+  a = fmaf(DCG_K2, m2 + p2, a);
+  a = fmaf(DCG_K3, m3 + p3, a);
+  a = fmaf(DCG_K4, m4 + p4, a);
+  return a;
+}
+
+// 8th-order first derivative (unscaled), weights L1..L4.
+__device__ __forceinline__ float d1w(float m1, float p1, float m2, float p2,
+                                     float m3, float p3, float m4, float p4) {
+  float a = DCG_L1 * (p1 - m1);
+  a = fmaf(DCG_L2, p2 - m2, a);
+  a = fmaf(DCG_L3, p3 - m3, a);
+  a = fmaf(DCG_L4, p4 - m4, a);
+  return a;
+}
+
+// Constant-angle factors of the reference CUDA backend
+// (include/sample_compute.h:9-18).
+constexpr float kCxx = 0.1459632909f, kCyy = 0.3540367091f, kCzz = 0.5f;
+constexpr float kCxy = 0.4546487134f, kCyz = 0.8414709848f;
+constexpr float kCxz = 0.5403023059f;
+constexpr float kV2pxFactor = 1.48f, kV2pnFactor = 1.2f;
+
+template <int TX, int TY, int NSTAGE, int MEDIUM, bool SPONGE>
+__global__ void __launch_bounds__(TX *TY, 1)
+    fast_kernel(const __grid_constant__ CUtensorMap tm_pc,
+                const __grid_constant__ CUtensorMap tm_qc,
+                const __grid_constant__ CUtensorMap tm_pp,
+                const __grid_constant__ CUtensorMap tm_qp,
+                const __grid_constant__ CUtensorMap tm_ca,
+                const __grid_constant__ CUtensorMap tm_cb,
+                const StepParams prm) {
+  using Lay = FastLayout<TX, TY, NSTAGE, MEDIUM>;
+  constexpr int HX = Lay::HX;
+  constexpr int NT = Lay::NT;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + Lay::OFF_BAR);
+
+  const int tid = threadIdx.x;
+  const int tx = tid % TX, ty = tid / TX;
+  const int x0 = prm.tile_x0 + static_cast<int>(blockIdx.x) * TX;
+  const int y0 = prm.tile_y0 + static_cast<int>(blockIdx.y) * TY;
+  const int zb = prm.z0 + static_cast<int>(blockIdx.z) * prm.zchunk;
+  const int ze = min(zb + prm.zchunk, prm.z1);
+  const int n_it = ze - zb + 2 * kHalo;
+  const int gx = x0 + tx, gy = y0 + ty;
+  const bool active =
+      gx >= prm.x0 && gx < prm.x1 && gy >= prm.y0 && gy < prm.y1;
+
+  if (tid == 0) {
+    for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
+    mbar_init_fence();
+    prefetch_tensormap(&tm_pc);
+    prefetch_tensormap(&tm_qc);
+    prefetch_tensormap(&tm_pp);
+    prefetch_tensormap(&tm_qp);
+    prefetch_tensormap(&tm_cb);
+    if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) prefetch_tensormap(&tm_ca);
+  }
+  __syncthreads();
+
+  // Producer: one elected thread fills stage j % NSTAGE for iteration j.
+  auto issue = [&](int j) {
+    const int s = j % NSTAGE;
+    unsigned char *st = smem + s * Lay::STAGE_BYTES;
+    const int k = zb - kHalo + j;
+    const bool want_ca = Lay::NCA > 0 && j >= kHalo && j < n_it - kHalo;
+    const bool want_out = j >= 2 * kHalo;
+    const uint32_t bytes = Lay::TX_HALO + (want_ca ? Lay::TX_CA : 0u) +
+                           (want_out ? Lay::TX_OUT : 0u);
+    mbar_arrive_expect_tx(&bars[s], bytes);
+    tma_load_3d(st + Lay::OFF_HP, &tm_pc, x0 - kHalo, y0 - kHalo, k, &bars[s]);
+    tma_load_3d(st + Lay::OFF_HQ, &tm_qc, x0 - kHalo, y0 - kHalo, k, &bars[s]);
+    if (want_ca) tma_load_4d(st + Lay::OFF_CA, &tm_ca, x0, y0, k, 0, &bars[s]);
+    if (want_out) {
+      tma_load_4d(st + Lay::OFF_CB, &tm_cb, x0, y0, k - kHalo,
+                  MEDIUM == DC_GB300_MEDIUM_PRECOMP ? 3 : 0, &bars[s]);
+      tma_load_3d(st + Lay::OFF_OWN, &tm_pp, x0, y0, k - kHalo, &bars[s]);
+      tma_load_3d(st + Lay::OFF_OWN + Lay::TILE_BYTES, &tm_qp, x0, y0,
+                  k - kHalo, &bars[s]);
+    }
+  };
+
+  if (tid == 0)
+    for (int j = 0; j < NSTAGE - 1 && j < n_it; ++j) issue(j);
+
+  // Register queues indexed by plane mod 9 (compile-time after unrolling).
+  float cqp[9], cqq[9], dxp[9], dxq[9], dyp[9], dyq[9];
+  float ap[9], bp[9], aq[9], bq[9];
+  float e_acc = 0.f;
+  int abort_it = -1;
+
+  // inactive threads of edge tiles may sit past the array: no profile read
+  const float gxy = (SPONGE && active)
+                        ? prm.sponge[gx] * prm.sponge[prm.sponge_oy + gy]
+                        : 1.0f;
+  const int c0 = (ty + kHalo) * HX + tx + kHalo;  // centre in a halo plane
+  const int od = ty * HX + tx + kHalo;            // centre in a dy plane
+  const int ot = ty * TX + tx;                    // centre in a tile
+
+  for (int it0 = 0; it0 < n_it; it0 += 9) {
+#pragma unroll
+    for (int u = 0; u < 9; ++u) {
+      const int it = it0 + u;
+      if (it < n_it) {  // CTA-uniform
+        const int s = it % NSTAGE;
+        const uint32_t par = static_cast<uint32_t>(it / NSTAGE) & 1u;
+        unsigned char *st = smem + s * Lay::STAGE_BYTES;
+        const bool ok = mbar_wait_bounded(&bars[s], par, kWaitLimitNs);
+        const float *hp = reinterpret_cast<const float *>(st + Lay::OFF_HP);
+        const float *hq = reinterpret_cast<const float *>(st + Lay::OFF_HQ);
+        float *dybp = reinterpret_cast<float *>(smem + Lay::OFF_DY +
+                                                (it & 1) * 2 * Lay::DY_BYTES);
+        float *dybq = dybp + Lay::DY_BYTES / 4;
+
+        // ---- leading plane k: centre, x/y second and first derivatives
+        float pxx, pyy, qxx, qyy;
+        {
+          const float *h = hp;
+          const float c = h[c0];
+          const float xm1 = h[c0 - 1], xp1 = h[c0 + 1], xm2 = h[c0 - 2],
+                      xp2 = h[c0 + 2], xm3 = h[c0 - 3], xp3 = h[c0 + 3],
+                      xm4 = h[c0 - 4], xp4 = h[c0 + 4];
+          const float ym1 = h[c0 - HX], yp1 = h[c0 + HX],
+                      ym2 = h[c0 - 2 * HX], yp2 = h[c0 + 2 * HX],
+                      ym3 = h[c0 - 3 * HX], yp3 = h[c0 + 3 * HX],
+                      ym4 = h[c0 - 4 * HX], yp4 = h[c0 + 4 * HX];
+          pxx = d2w(c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4) * prm.dxxinv;
+          pyy = d2w(c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4) * prm.dyyinv;
+          cqp[u] = c;
+          dxp[u] = d1w(xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
+          dyp[u] = d1w(ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
+          dybp[od] = dyp[u];
+        }
+        {
+          const float *h = hq;
+          const float c = h[c0];
+          const float xm1 = h[c0 - 1], xp1 = h[c0 + 1], xm2 = h[c0 - 2],
+                      xp2 = h[c0 + 2], xm3 = h[c0 - 3], xp3 = h[c0 + 3],
+                      xm4 = h[c0 - 4], xp4 = h[c0 + 4];
+          const float ym1 = h[c0 - HX], yp1 = h[c0 + HX],
+                      ym2 = h[c0 - 2 * HX], yp2 = h[c0 + 2 * HX],
+                      ym3 = h[c0 - 3 * HX], yp3 = h[c0 + 3 * HX],
+                      ym4 = h[c0 - 4 * HX], yp4 = h[c0 + 4 * HX];
+          qxx = d2w(c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4) * prm.dxxinv;
+          qyy = d2w(c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4) * prm.dyyinv;
+          cqq[u] = c;
+          dxq[u] = d1w(xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
+          dyq[u] = d1w(ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
+          dybq[od] = dyq[u];
+        }
+        // y-derivatives of the 4 + 4 halo columns (needed by d2/dxdy)
+        if (tid < 8 * TY) {
+          const int hc = tid & 7, hy = tid >> 3;
+          const int hx = hc < 4 ? hc : TX + hc;
+          const int o = (hy + kHalo) * HX + hx;
+          dybp[hy * HX + hx] =
+              d1w(hp[o - HX], hp[o + HX], hp[o - 2 * HX], hp[o + 2 * HX],
+                  hp[o - 3 * HX], hp[o + 3 * HX], hp[o - 4 * HX],
+                  hp[o + 4 * HX]);
+          dybq[hy * HX + hx] =
+              d1w(hq[o - HX], hq[o + HX], hq[o - 2 * HX], hq[o + 2 * HX],
+                  hq[o - 3 * HX], hq[o + 3 * HX], hq[o - 4 * HX],
+                  hq[o + 4 * HX]);
+        }
+        if (__syncthreads_or(!ok)) {
+          abort_it = it;
+          goto done;
+        }
+        // The slot read in iteration it-1 is free: refill it.
+        if (tid == 0 && it + NSTAGE - 1 < n_it) issue(it + NSTAGE - 1);
+
+        // ---- in-plane part of H1/H2 at plane k, delayed to output time
+        if (it >= kHalo && it < n_it - kHalo) {
+          const float pxy = d1w(dybp[od - 1], dybp[od + 1], dybp[od - 2],
+                                dybp[od + 2], dybp[od - 3], dybp[od + 3],
+                                dybp[od - 4], dybp[od + 4]) *
+                            prm.dxyinv;
+          const float qxy = d1w(dybq[od - 1], dybq[od + 1], dybq[od - 2],
+                                dybq[od + 2], dybq[od - 3], dybq[od + 3],
+                                dybq[od - 4], dybq[od + 4]) *
+                            prm.dxyinv;
+          float cxx, cyy, cxy;
+          if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) {
+            const float *ca = reinterpret_cast<const float *>(st + Lay::OFF_CA);
+            cxx = ca[ot];
+            cyy = ca[NT + ot];
+            cxy = ca[2 * NT + ot];
+          } else {
+            cxx = kCxx;
+            cyy = kCyy;
+            cxy = kCxy;
+          }
+          ap[u] = fmaf(cxy, pxy, fmaf(cyy, pyy, cxx * pxx));
+          bp[u] = pxx + pyy;
+          aq[u] = fmaf(cxy, qxy, fmaf(cyy, qyy, cxx * qxx));
+          bq[u] = qxx + qyy;
+        }
+
+        // ---- output plane z = k - 4
+        if (it >= 2 * kHalo) {
+          const int z = zb + it - 2 * kHalo;
+          // ring slots of planes z-4 .. z+4 (u is a compile-time constant)
+          const int m4 = (u + 1) % 9, m3 = (u + 2) % 9, m2 = (u + 3) % 9,
+                    m1 = (u + 4) % 9, c = (u + 5) % 9, p1 = (u + 6) % 9,
+                    p2 = (u + 7) % 9, p3 = (u + 8) % 9, p4 = u;
+          const float pzz = d2w(cqp[c], cqp[m1], cqp[p1], cqp[m2], cqp[p2],
+                                cqp[m3], cqp[p3], cqp[m4], cqp[p4]) *
+                            prm.dzzinv;
+          const float qzz = d2w(cqq[c], cqq[m1], cqq[p1], cqq[m2], cqq[p2],
+                                cqq[m3], cqq[p3], cqq[m4], cqq[p4]) *
+                            prm.dzzinv;
+          const float pxz = d1w(dxp[m1], dxp[p1], dxp[m2], dxp[p2], dxp[m3],
+                                dxp[p3], dxp[m4], dxp[p4]) *
+                            prm.dxzinv;
+          const float qxz = d1w(dxq[m1], dxq[p1], dxq[m2], dxq[p2], dxq[m3],
+                                dxq[p3], dxq[m4], dxq[p4]) *
+                            prm.dxzinv;
+          const float pyz = d1w(dyp[m1], dyp[p1], dyp[m2], dyp[p2], dyp[m3],
+                                dyp[p3], dyp[m4], dyp[p4]) *
+                            prm.dyzinv;
+          const float qyz = d1w(dyq[m1], dyq[p1], dyq[m2], dyq[p2], dyq[m3],
+                                dyq[p3], dyq[m4], dyq[p4]) *
+                            prm.dyzinv;
+          const float *cb = reinterpret_cast<const float *>(st + Lay::OFF_CB);
+          const float *own = reinterpret_cast<const float *>(st + Lay::OFF_OWN);
+          float czz, cxz, cyz, v2px, v2pz, v2sz, v2pn;
+          if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) {
+            czz = cb[0 * NT + ot];
+            cxz = cb[1 * NT + ot];
+            cyz = cb[2 * NT + ot];
+            v2px = cb[3 * NT + ot];
+            v2pz = cb[4 * NT + ot];
+            v2sz = cb[5 * NT + ot];
+            v2pn = cb[6 * NT + ot];
+          } else {
+            const float vp = cb[ot], vs = cb[NT + ot];
+            czz = kCzz;
+            cxz = kCxz;
+            cyz = kCyz;
+            v2pz = vp * vp;
+            v2sz = vs * vs;
+            v2px = v2pz * kV2pxFactor;
+            v2pn = v2pz * kV2pnFactor;
+          }
+          const float h1p = fmaf(cyz, pyz, fmaf(cxz, pxz, fmaf(czz, pzz, ap[c])));
+          const float h2p = bp[c] + pzz - h1p;
+          const float h1q = fmaf(cyz, qyz, fmaf(cxz, qxz, fmaf(czz, qzz, aq[c])));
+          const float h2q = bq[c] + qzz - h1q;
+          const float rhsp =
+              fmaf(v2sz, h1p - h1q, fmaf(v2pz, h1q, v2px * h2p));
+          const float rhsq =
+              fmaf(-v2sz, h2p - h2q, fmaf(v2pz, h1q, v2pn * h2p));
+          const float ppo = own[ot], qpo = own[NT + ot];
+          float np, nq;
+          if (SPONGE) {
+            const float g = gxy * prm.sponge[prm.sponge_oz + z];
+            np = fmaf(rhsp, prm.dt2, fmaf(-g, ppo, 2.0f * cqp[c])) * g;
+            nq = fmaf(rhsq, prm.dt2, fmaf(-g, qpo, 2.0f * cqq[c])) * g;
+          } else {
+            np = fmaf(rhsp, prm.dt2, 2.0f * cqp[c] - ppo);
+            nq = fmaf(rhsq, prm.dt2, 2.0f * cqq[c] - qpo);
+          }
+          if (active) {
+            const long long gi = static_cast<long long>(z) * prm.plane +
+                                 static_cast<long long>(gy) * prm.pitch + gx;
+            if (prm.energy) e_acc = fmaf(np, np, fmaf(nq, nq, e_acc));
+            if (gx == prm.src_x && gy == prm.src_y && z == prm.src_z) {
+              const int step = *prm.d_step + prm.step_offset;
+              const float sv =
+                  step + 1 < prm.src_count ? prm.src_table[step + 1] : 0.0f;
+              prm.src_pre[0] = np;
+              prm.src_pre[1] = nq;
+              np += sv;
+              nq += sv;
+            }
+            prm.pp_out[gi] = np;
+            prm.qp_out[gi] = nq;
+          }
+        }
+      }
+    }
+  }
+done:
+  if (abort_it >= 0) {
+    // A TMA wait timed out: record it, give the copies still in flight a
+    // bounded chance to land, and leave without touching the outputs.
+    if (tid == 0) {
+      atomicOr(prm.err, kErrTimeout);
+      const int last = min(n_it, abort_it + NSTAGE - 1);
+      for (int j = abort_it; j < last; ++j)
+        mbar_wait_bounded(&bars[j % NSTAGE],
+                          static_cast<uint32_t>(j / NSTAGE) & 1u, kWaitLimitNs);
+    }
+    return;
+  }
+  if (prm.energy) {
+    // CTA reduction of the float partials in double, one atomic per CTA.
+    double e = static_cast<double>(e_acc);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) e += __shfl_down_sync(0xffffffffu, e, off);
+    double *red = reinterpret_cast<double *>(smem + Lay::OFF_DY);
+    __syncthreads();
+    if ((tid & 31) == 0) red[tid >> 5] = e;
+    __syncthreads();
+    if (tid == 0) {
+      double tot = 0.0;
+      for (int w = 0; w < NT / 32; ++w) tot += red[w];
+      const int step = *prm.d_step + prm.step_offset;
+      if (step >= 0 && step < prm.energy_cap) atomicAdd(&prm.energy[step], tot);
+    }
+  }
+}
+
+// Compiled tile shape.  TX = 32 (one warp per tile row), TY = 16 rows,
+// a 4-stage TMA ring; see the design doc for the choice.
+constexpr int kTX = 32, kTY = 16, kStages = 4;
+
+template <int MEDIUM, bool SPONGE>
+cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int pc_buf,
+                          int qc_buf, int pp_buf, int qp_buf) {
+  using Lay = FastLayout<kTX, kTY, kStages, MEDIUM>;
+  auto kern = fast_kernel<kTX, kTY, kStages, MEDIUM, SPONGE>;
+  const int nx = prm.x1 - prm.tile_x0, ny = prm.y1 - prm.tile_y0;
+  const int nz = prm.z1 - prm.z0;
+  dim3 grid((nx + kTX - 1) / kTX, (ny + kTY - 1) / kTY,
+            (nz + prm.zchunk - 1) / prm.zchunk);
+  const CUtensorMap &cb = sim->tm_cb;
+  kern<<<grid, kTX * kTY, Lay::SMEM_BYTES, sim->stream>>>(
+      sim->tm_halo[pc_buf], sim->tm_halo[qc_buf], sim->tm_own[pp_buf],
+      sim->tm_own[qp_buf], sim->tm_ca, cb, prm);
+  return cudaGetLastError();
+}
+
+template <int MEDIUM, bool SPONGE>
+cudaError_t set_smem_attr() {
+  using Lay = FastLayout<kTX, kTY, kStages, MEDIUM>;
+  return cudaFuncSetAttribute(fast_kernel<kTX, kTY, kStages, MEDIUM, SPONGE>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM_BYTES);
+}
+
+}  // namespace
+
+FastShape fast_shape(const Sim *sim) {
+  // z-chunk: enough CTAs for several waves over 152 SMs while keeping the
+  // 8-plane warm-up of each chunk small.
+  const long long tiles = ((sim->sx - 8 + kTX - 1) / kTX + 1) *
+                          ((sim->sy - 8 + kTY - 1) / kTY);
+  const long long nzc = sim->sz - 8;
+  long long chunks = (4 * 152 + tiles - 1) / tiles;
+  long long zc = (nzc + chunks - 1) / chunks;
+  if (zc < 32) zc = 32;
+  if (zc > nzc) zc = nzc;
+  return FastShape{kTX, kTY, static_cast<int>(zc)};
+}
+
+bool fast_encode_maps(Sim *sim, std::string *err) {
+  // dynamic shared memory above 48 KB must be enabled per kernel and device
+  // (done here, before any stream capture)
+  cudaError_t ae = sim->medium == DC_GB300_MEDIUM_PRECOMP
+                       ? set_smem_attr<DC_GB300_MEDIUM_PRECOMP, false>()
+                       : set_smem_attr<DC_GB300_MEDIUM_VPZ_VSV, false>();
+  if (ae == cudaSuccess)
+    ae = sim->medium == DC_GB300_MEDIUM_PRECOMP ? set_smem_attr<DC_GB300_MEDIUM_PRECOMP, true>()
+                                                : set_smem_attr<DC_GB300_MEDIUM_VPZ_VSV, true>();
+  if (ae != cudaSuccess) {
+    *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(ae);
+    return false;
+  }
+  const uint64_t dims3[3] = {static_cast<uint64_t>(sim->sx),
+                             static_cast<uint64_t>(sim->sy),
+                             static_cast<uint64_t>(sim->sz)};
+  const uint64_t str3[2] = {static_cast<uint64_t>(sim->pitch) * 4,
+                            static_cast<uint64_t>(sim->plane) * 4};
+  const uint32_t box_halo[3] = {kTX + 8, kTY + 8, 1};
+  const uint32_t box_own[3] = {kTX, kTY, 1};
+  for (int b = 0; b < 4; ++b) {
+    if (!encode_tiled(&sim->tm_halo[b], sim->field[b], 3, dims3, str3, box_halo, err))
+      return false;
+    if (!encode_tiled(&sim->tm_own[b], sim->field[b], 3, dims3, str3, box_own, err))
+      return false;
+  }
+  const uint64_t str4[3] = {str3[0], str3[1],
+                            static_cast<uint64_t>(sim->count) * 4};
+  if (sim->medium == DC_GB300_MEDIUM_PRECOMP) {
+    const uint64_t dims4[4] = {dims3[0], dims3[1], dims3[2], DC_NCOEF};
+    const uint32_t box_a[4] = {kTX, kTY, 1, 3};
+    const uint32_t box_b[4] = {kTX, kTY, 1, 7};
+    if (!encode_tiled(&sim->tm_ca, sim->coef, 4, dims4, str4, box_a, err)) return false;
+    if (!encode_tiled(&sim->tm_cb, sim->coef, 4, dims4, str4, box_b, err)) return false;
+  } else {
+    const uint64_t dims4[4] = {dims3[0], dims3[1], dims3[2], 2};
+    const uint32_t box_b[4] = {kTX, kTY, 1, 2};
+    if (!encode_tiled(&sim->tm_cb, sim->vv, 4, dims4, str4, box_b, err)) return false;
+    sim->tm_ca = sim->tm_cb;  // unused by this medium form
+  }
+  sim->maps_tx = kTX;
+  sim->maps_ty = kTY;
+  return true;
+}
+
+cudaError_t launch_fast(Sim *sim, const StepParams &prm, int pc_buf,
+                        int qc_buf, int pp_buf, int qp_buf) {
+  const bool sp = prm.sponge != nullptr;
+  if (sim->medium == DC_GB300_MEDIUM_PRECOMP)
+    return sp ? launch_fast_t<DC_GB300_MEDIUM_PRECOMP, true>(sim, prm, pc_buf, qc_buf, pp_buf, qp_buf)
+              : launch_fast_t<DC_GB300_MEDIUM_PRECOMP, false>(sim, prm, pc_buf, qc_buf, pp_buf, qp_buf);
+  return sp ? launch_fast_t<DC_GB300_MEDIUM_VPZ_VSV, true>(sim, prm, pc_buf, qc_buf, pp_buf, qp_buf)
+            : launch_fast_t<DC_GB300_MEDIUM_VPZ_VSV, false>(sim, prm, pc_buf, qc_buf, pp_buf, qp_buf);
+}
+
+}  // namespace dcg

@@ -1,0 +1,331 @@
+/*
+ * dc_gb300.h -- C ABI of libdc_gb300.so, a GB300-native (sm_103a) Fletcher
+ * TTI pseudo-acoustic propagator that drops in for the time-step path of
+ * Dannful/distributed-cube-average.
+ *
+ * Part 1 re-declares the reference's own entry points and ABI structs with
+ * identical signatures and layouts, so the reference's host code (src/
+ * worker.c, src/main.c) links against this library in place of its CUDA or
+ * OpenMP backend (reference Makefile:30-60 picks one backend at link time).
+ * Each declaration cites the reference declaration it replaces.
+ *
+ * Part 2 is this library's own API (dc_gb300_*): status-returning, one
+ * stream per simulation, multi-step runs captured in CUDA graphs, fused
+ * source injection, sponge, receivers and energy.
+ *
+ * Conventions shared by both parts:
+ *   - arrays are x fastest: index = x + y*sx + z*sx*sy
+ *     (reference include/indexing.h:15-21); sizes include the 4-cell stencil
+ *     halo (include/definitions.h:4);
+ *   - only points in [4, s-4) per axis are ever updated.
+ */
+#ifndef DC_GB300_H
+#define DC_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ====================================================================== */
+/* Part 1 -- the reference ABI                                            */
+/* ====================================================================== */
+
+#ifndef DC_GB300_NO_REFERENCE_TYPES
+/* include/precomp.h:6-17 */
+typedef struct {
+  float *ch1dxx;
+  float *ch1dyy;
+  float *ch1dzz;
+  float *ch1dxy;
+  float *ch1dyz;
+  float *ch1dxz;
+  float *v2px;
+  float *v2pz;
+  float *v2sz;
+  float *v2pn;
+} dc_precomp_vars;
+
+/* include/precomp.h:19-26 */
+typedef struct {
+  float *theta;
+  float *phi;
+  float *vsv;
+  float *vpz;
+  float *epsilon;
+  float *delta;
+} dc_anisotropy_t;
+
+/* include/dc_process.h:7-21 (DIMENSIONS = 3, NEIGHBOURHOOD = 27) */
+typedef struct {
+  int rank;
+  int coordinates[3];
+  int neighbours[27];
+  int topology[3];
+  unsigned int iterations;
+  int source_index;
+  float dx, dy, dz, dt;
+  size_t sizes[3];
+  dc_anisotropy_t anisotropy_vars;
+  dc_precomp_vars precomp_vars;
+  float *pp, *pc, *qp, *qc;
+  char *hostnames;
+  size_t num_workers;
+} dc_process_t;
+
+/* include/device_data.h:11-15.  The field and medium pointers are device
+ * pointers into this library's arrays.  Rows of a device array are `pitch`
+ * floats apart, where pitch = sx rounded up to a multiple of 4 (pitch == sx
+ * whenever sx % 4 == 0); dc_gb300_device_pitch() returns it. */
+typedef struct {
+  float *pp, *pc, *qp, *qc;
+  float *vpz, *vsv;
+  dc_precomp_vars precomp_vars;
+} dc_device_data;
+#endif /* DC_GB300_NO_REFERENCE_TYPES */
+
+/* include/propagate.h:13-18 -- src/cuda_propagate.cu:32-69.
+ * Updates pp/qp in place for every point of the half-open box
+ * [start_coords, end_coords) of an array of extent `sizes`.
+ * process_coordinates/topology are accepted and ignored, as in the
+ * reference (include/sample_compute.h:23-25).  Launches asynchronously on
+ * the simulation's stream (the reference synchronises after every call);
+ * dc_device_data_get_results synchronises.  A box outside [4, size-4) or
+ * sizes that differ from the ones given to dc_device_data_init print an
+ * error and exit(1), like the reference's error path. */
+void dc_propagate(const size_t start_coords[3], const size_t end_coords[3],
+                  const size_t sizes[3], const int process_coordinates[3],
+                  const int topology[3], dc_device_data *data, const float dx,
+                  const float dy, const float dz, const float dt);
+
+/* include/device_data.h:17 -- src/device_data.cu:35-94.
+ * Allocates the device arrays and copies pp, pc, qp, qc and the medium from
+ * the process.  The medium comes from process->precomp_vars (all ten arrays)
+ * when ch1dxx is non-NULL, else from process->anisotropy_vars (the trig
+ * precompute then runs on the GPU in FP64).  vpz/vsv are copied when
+ * present.  Selects CUDA device 0 unless DC_GB300_DEVICE is set (the
+ * reference picks by hostname rank, src/device_data.cu:18-33).
+ * Environment: DC_GB300_KERNEL=fast|exact selects the stencil arithmetic;
+ * DC_GB300_MEDIUM=precomp|vpz_vsv selects the medium form (vpz_vsv = the
+ * reference CUDA backend's constant-angle arithmetic,
+ * include/sample_compute.h:9-18). */
+dc_device_data *dc_device_data_init(dc_process_t *process);
+
+/* include/device_data.h:19 -- src/device_data.cu:96-105 */
+void dc_device_data_free(dc_device_data *data);
+
+/* include/device_data.h:21 -- src/device_data.cu:107-117.
+ * Waits for all queued work, then copies pc and qc to process->pc/qc. */
+void dc_device_data_get_results(dc_process_t *process, dc_device_data *data);
+
+/* include/device_data.h:23 -- src/device_data.cu:119-129: pointer swap
+ * pp<->pc, qp<->qc (host side; no device work). */
+void dc_device_swap_arrays(dc_device_data *data);
+
+/* include/device_data.h:25 -- src/device_data.cu:131-139:
+ * pc[index] += source; qc[index] += source (queued on the stream). */
+void dc_device_add_source(dc_device_data *data, size_t index, float source);
+
+/* include/device_data.h:27-31 -- src/device_data.cu:141-161.  Copies the
+ * box [start,end) of the device array `from_array` into the dense host
+ * buffer (x fastest).  Synchronous. */
+void dc_device_extract_halo_face(dc_device_data *data, float *buffer,
+                                 const size_t start_coords[3],
+                                 const size_t end_coords[3],
+                                 const size_t sizes[3],
+                                 const float *from_array);
+
+/* include/device_data.h:33-37 -- src/device_data.cu:163-183.  Copies the
+ * dense host buffer into the box [start,end) of `to_array`.  Synchronous. */
+void dc_device_insert_halo_face(dc_device_data *data, const float *buffer,
+                                const size_t start_coords[3],
+                                const size_t end_coords[3],
+                                const size_t sizes[3], float *to_array);
+
+/* include/precomp.h:28-29 -- src/precomp.c:9-108.  Host arrays (malloc'd,
+ * freed with dc_free_precomp_vars).  The trigonometry runs on the GPU in
+ * FP64 and is rounded to float as the reference rounds its host libm
+ * results. */
+dc_precomp_vars dc_compute_precomp_vars(int sx, int sy, int sz,
+                                        dc_anisotropy_t anisotropy);
+
+/* include/precomp.h:30 -- src/precomp.c:110-171: default homogeneous
+ * medium (vpz 3000, eps 0.24, delta 0.10, phi 1 rad, theta pi/4, SIGMA
+ * rule for vsv), malloc'd host arrays. */
+dc_anisotropy_t dc_compute_anisotropy_vars(int sx, int sy, int sz);
+
+/* include/precomp.h:31 -- src/precomp.c:189-211 */
+void dc_free_precomp_vars(dc_precomp_vars *vars);
+
+/* include/precomp.h:32 -- src/precomp.c:173-187 */
+void dc_free_anisotropy_vars(dc_anisotropy_t *anisotropy);
+
+/* include/boundary.h:5-12 -- src/boundary.c:7-104: random velocity
+ * boundary on host arrays, same glibc rand_r sequence. */
+void randomVelocityBoundaryPartition(int local_sx, int local_sy, int local_sz,
+                                     int global_sx, int global_sy,
+                                     int global_sz, int start_x, int start_y,
+                                     int start_z, int nx, int ny, int nz,
+                                     int bord, int absorb, float *vpz,
+                                     float *vsv, unsigned int *seed);
+
+/* include/calculate_source.h:3 -- src/calculate_source.c:10-17 (FCUT=40). */
+float dc_calculate_source(float dt, int it);
+
+/* ====================================================================== */
+/* Part 2 -- this library's own API                                       */
+/* ====================================================================== */
+
+/* Status codes. */
+enum {
+  DC_GB300_OK = 0,
+  DC_GB300_ERR_ARG = 1,     /* invalid argument (size, box, pointer) */
+  DC_GB300_ERR_CUDA = 2,    /* a CUDA runtime/driver call failed */
+  DC_GB300_ERR_NOMEM = 3,   /* allocation failed */
+  DC_GB300_ERR_DEVICE = 4,  /* no usable sm_103 device */
+  DC_GB300_ERR_TIMEOUT = 5, /* a bounded device wait gave up */
+  DC_GB300_ERR_STATE = 6    /* call not valid in the current state */
+};
+
+/* Stencil arithmetic. */
+enum {
+  DC_GB300_KERNEL_FAST = 0,  /* separable cross derivatives, FMA */
+  DC_GB300_KERNEL_EXACT = 1  /* the reference's operation order, no FMA:
+                                bit-identical to the reference OpenMP path */
+};
+
+/* Medium form read by the stencil. */
+enum {
+  DC_GB300_MEDIUM_PRECOMP = 0, /* ten coefficient arrays (64 B/update) */
+  DC_GB300_MEDIUM_VPZ_VSV = 1  /* vpz/vsv + the reference CUDA backend's
+                                  constant angles (32 B/update) */
+};
+
+typedef struct dc_gb300_sim dc_gb300_sim;
+
+typedef struct {
+  long sx, sy, sz;          /* padded sizes incl. 4-cell halo, each >= 9 */
+  float dx, dy, dz, dt;
+  int kernel;               /* DC_GB300_KERNEL_* */
+  int medium;               /* DC_GB300_MEDIUM_* */
+  int device;               /* CUDA ordinal; < 0 = current device */
+} dc_gb300_config;
+
+/* Last error message of the calling thread ("" if none). */
+const char *dc_gb300_last_error(void);
+
+/* Library version string. */
+const char *dc_gb300_version(void);
+
+int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out);
+void dc_gb300_destroy(dc_gb300_sim *sim);
+
+/* The reference-ABI view of a simulation (shares its arrays). */
+dc_device_data *dc_gb300_device_data(dc_gb300_sim *sim);
+/* The simulation behind a dc_device_data from dc_device_data_init. */
+dc_gb300_sim *dc_gb300_from_device_data(dc_device_data *data);
+long dc_gb300_device_pitch(const dc_gb300_sim *sim);
+
+/* Medium from dense host arrays (sx*sy*sz floats each). */
+int dc_gb300_set_precomp(dc_gb300_sim *sim, const dc_precomp_vars *host);
+int dc_gb300_set_vpz_vsv(dc_gb300_sim *sim, const float *vpz,
+                         const float *vsv);
+/* Uploads theta, phi, vsv, vpz, epsilon, delta and runs the FP64 trig
+ * precompute of src/precomp.c:85-105 on the GPU. */
+int dc_gb300_set_anisotropy(dc_gb300_sim *sim, const dc_anisotropy_t *host);
+
+/* Copies the device medium back to dense host arrays (sx*sy*sz floats
+ * each; NULL members are skipped).  Synchronous. */
+int dc_gb300_get_precomp(dc_gb300_sim *sim, const dc_precomp_vars *host);
+int dc_gb300_get_vpz_vsv(dc_gb300_sim *sim, float *vpz, float *vsv);
+
+/* Seeded layered medium generated on the GPU (see dc_gb300_layered_spec). */
+#define DC_GB300_MAX_LAYERS 32
+#define DC_GB300_MAX_FEATURES 128
+typedef struct {
+  int nlayers;
+  float layer_top[DC_GB300_MAX_LAYERS]; /* first global z of each layer */
+  float vp[DC_GB300_MAX_LAYERS];
+  float epsilon[DC_GB300_MAX_LAYERS];
+  float delta[DC_GB300_MAX_LAYERS];
+  float vp_noise;                   /* relative amplitude (0.02 = 2 %) */
+  float theta_lo, theta_hi;         /* marginal range of theta */
+  float phi_lo, phi_hi;             /* marginal range of phi */
+  float sigma_ratio;                /* vsv = vp*sqrt(|eps-delta|/ratio) */
+  /* random Fourier features: field = sqrt(2/n) sum cos(k.r + ph) with
+   * k = (kx,ky,kz) in radians per cell and r the global cell index */
+  int n_noise, n_theta, n_phi;
+  float k_noise[DC_GB300_MAX_FEATURES][4];  /* kx, ky, kz, phase */
+  float k_theta[DC_GB300_MAX_FEATURES][4];
+  float k_phi[DC_GB300_MAX_FEATURES][4];
+  /* global origin of this array inside a larger model (crops) */
+  long ox, oy, oz;
+} dc_gb300_layered_spec;
+int dc_gb300_generate_layered(dc_gb300_sim *sim,
+                              const dc_gb300_layered_spec *spec);
+
+/* Fields from dense host arrays; NULL means zeros.  Resets the step
+ * counter to 0. */
+int dc_gb300_set_fields(dc_gb300_sim *sim, const float *pp, const float *pc,
+                        const float *qp, const float *qc);
+/* Copies the fields to dense host arrays (NULL skips one).  Synchronous. */
+int dc_gb300_get_fields(dc_gb300_sim *sim, float *pp, float *pc, float *qp,
+                        float *qc);
+
+/* Point source at linear index `index`: before step it, amplitudes[it] is
+ * added to pc and qc (src/worker.c:467-470); steps beyond `count` add 0.
+ * index < 0 removes the source. */
+int dc_gb300_set_source(dc_gb300_sim *sim, long index,
+                        const float *amplitudes, int count);
+
+/* Sponge: after each update the new value is multiplied by
+ * g = gx[x]*gy[y]*gz[z] and the previous field is damped by g before use.
+ * NULL pointers remove it. */
+int dc_gb300_set_sponge(dc_gb300_sim *sim, const float *gx, const float *gy,
+                        const float *gz);
+
+/* Receivers: after step it, trace[it*count + r] = p at index[r] (the new
+ * field, before the next step's source).  Capacity max_steps rows. */
+int dc_gb300_set_receivers(dc_gb300_sim *sim, const long *index, int count,
+                           int max_steps);
+int dc_gb300_get_traces(dc_gb300_sim *sim, float *out, int steps);
+
+/* Energy: after step it, energy[it] = sum(p^2 + q^2) over [4,s-4)^3 of the
+ * new fields, accumulated in FP64 across blocks. */
+int dc_gb300_enable_energy(dc_gb300_sim *sim, int max_steps);
+int dc_gb300_get_energy(dc_gb300_sim *sim, double *out, int steps);
+
+/* Advances `steps` time steps (source -> stencil over [4,s-4)^3 -> swap),
+ * queued on the simulation's stream; runs of >= 2 steps are replayed from
+ * a captured CUDA graph. */
+int dc_gb300_run(dc_gb300_sim *sim, int steps);
+int dc_gb300_synchronize(dc_gb300_sim *sim);
+long dc_gb300_steps_done(const dc_gb300_sim *sim);
+
+/* One stencil pass over a box without source or swap (the dc_propagate
+ * semantics, status-returning). */
+int dc_gb300_propagate_box(dc_gb300_sim *sim, const size_t start[3],
+                           const size_t end[3]);
+
+/* Kernel launches issued by this simulation so far (stencil + helpers). */
+long dc_gb300_kernel_launches(const dc_gb300_sim *sim);
+
+/* Stream of the simulation (a cudaStream_t) for event timing. */
+void *dc_gb300_stream(dc_gb300_sim *sim);
+
+/* The wavelet of dc_calculate_source with the cut-off frequency as a
+ * parameter (the reference fixes FCUT = 40, src/calculate_source.c:5); the
+ * Ricker peak frequency is fcut / 3. */
+float dc_gb300_source(float dt, int it, double fcut);
+
+/* Sponge profile along one axis of padded size s with absorbing width a:
+ * g[i] = exp(-(kappa*d/a)^2), d = cells into the shell (1 next to the
+ * physical interior .. a next to the halo), 1 elsewhere. */
+void dc_gb300_sponge_profile(long s, long a, double kappa, float *g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DC_GB300_H */
