@@ -42,7 +42,7 @@ constexpr int kRefToDev[10] = {DC_CXX, DC_CYY, DC_CZZ, DC_CXY, DC_CYZ,
 constexpr int kHalo = 4;  // stencil radius (include/definitions.h:4)
 
 // Error word bits written by kernels.
-enum : int { kErrTimeout = 1 };
+enum : int { kErrTimeout = 1, kErrAlign = 2 };
 
 struct StepParams {
   int x0, x1, y0, y1, z0, z1;   // half-open box of updated points
@@ -50,6 +50,9 @@ struct StepParams {
   int zchunk;                   // output planes per block
   long long pitch, plane;       // floats between rows / planes
   float dxxinv, dyyinv, dzzinv, dxyinv, dxzinv, dyzinv;
+  // fast kernel: FD weights pre-scaled by the grid spacing
+  float w2x[5], w2y[5], w2z[5];  // K_i / da^2 (second derivative)
+  float w1x[4], w1y[4], w1z[4];  // L_i / da   (first derivative, i = 1..4)
   float dt, dt2;
   float *pp_out, *qp_out;       // pp/qp buffers (read, then written in place)
   const float *pc_in, *qc_in;   // current fields (exact kernel reads these)

@@ -128,6 +128,21 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
   p.dxyinv = 1.0f / (dx * dy);
   p.dxzinv = 1.0f / (dx * dz);
   p.dyzinv = 1.0f / (dy * dz);
+  {
+    const double K[5] = {-205.0 / 72.0, 8.0 / 5.0, -1.0 / 5.0, 8.0 / 315.0, -1.0 / 560.0};
+    const double L[4] = {4.0 / 5.0, -1.0 / 5.0, 4.0 / 105.0, -1.0 / 280.0};
+    const double hx = dx, hy = dy, hz = dz;
+    for (int k = 0; k < 5; ++k) {
+      p.w2x[k] = static_cast<float>(K[k] / (hx * hx));
+      p.w2y[k] = static_cast<float>(K[k] / (hy * hy));
+      p.w2z[k] = static_cast<float>(K[k] / (hz * hz));
+    }
+    for (int k = 0; k < 4; ++k) {
+      p.w1x[k] = static_cast<float>(L[k] / hx);
+      p.w1y[k] = static_cast<float>(L[k] / hy);
+      p.w1z[k] = static_cast<float>(L[k] / hz);
+    }
+  }
   p.dt = dt;
   p.dt2 = dt * dt;
   const dc_device_data &a = s->handle->abi;
@@ -200,10 +215,11 @@ int check_err_word(Sim *s) {
   int h = 0;
   DCG_TRY(cudaMemcpyAsync(&h, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   DCG_TRY(cudaStreamSynchronize(s->stream));
-  if (h & kErrTimeout) {
-    cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
+  if (h) cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
+  if (h & kErrTimeout)
     return fail(DC_GB300_ERR_TIMEOUT, "a TMA wait in the stencil kernel timed out");
-  }
+  if (h & kErrAlign)
+    return fail(DC_GB300_ERR_CUDA, "shared-memory window not 128-byte aligned");
   return DC_GB300_OK;
 }
 

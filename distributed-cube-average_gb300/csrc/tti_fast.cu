@@ -53,36 +53,38 @@ struct FastLayout {
   static constexpr int OFF_OWN = OFF_CB + NCB * TILE_BYTES;
   static constexpr int STAGE_BYTES = OFF_OWN + 2 * TILE_BYTES;
   static constexpr int DY_BYTES = align128(TY * HX * 4);
-  static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;  // [parity][field]
-  static constexpr int OFF_BAR = OFF_DY + 4 * DY_BYTES;
-  static constexpr int SMEM_BYTES = OFF_BAR + NSTAGE * 8 + 128;
+  static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;  // [3 buffers][field]
+  static constexpr int OFF_BAR = OFF_DY + 3 * 2 * DY_BYTES;
+  static constexpr int SMEM_BYTES = OFF_BAR + NSTAGE * 8;
   static constexpr uint32_t TX_HALO = 2u * HX * HY * 4u;
   static constexpr uint32_t TX_CA = NCA * NT * 4u;
   static constexpr uint32_t TX_OUT = (NCB + 2) * NT * 4u;
   static_assert(TX % 32 == 0, "a warp spans one tile row");
   static_assert(HX * 4 % 16 == 0, "TMA box rows are 16-byte multiples");
   static_assert(8 * TY <= NT, "halo-column work fits the CTA");
+  static_assert(NSTAGE == 3, "stage index u % 3 is a compile-time constant");
 };
 
-// 8th-order second derivative (unscaled), weights K0..K4.
-__device__ __forceinline__ float d2w(float c, float m1, float p1, float m2,
-                                     float p2, float m3, float p3, float m4,
-                                     float p4) {
-  float a = DCG_K0 * c;
-  a = fmaf(DCG_K1, m1 + p1, a);
-  a = fmaf(DCG_K2, m2 + p2, a);
-  a = fmaf(DCG_K3, m3 + p3, a);
-  a = fmaf(DCG_K4, m4 + p4, a);
+// Second derivative with pre-scaled weights w[0..4] (K_i / da^2).
+__device__ __forceinline__ float d2w(const float *w, float c, float m1,
+                                     float p1, float m2, float p2, float m3,
+                                     float p3, float m4, float p4) {
+  float a = w[0] * c;
+  a = fmaf(w[1], m1 + p1, a);
+  a = fmaf(w[2], m2 + p2, a);
+  a = fmaf(w[3], m3 + p3, a);
+  a = fmaf(w[4], m4 + p4, a);
   return a;
 }
 
-// 8th-order first derivative (unscaled), weights L1..L4.
-__device__ __forceinline__ float d1w(float m1, float p1, float m2, float p2,
-                                     float m3, float p3, float m4, float p4) {
-  float a = DCG_L1 * (p1 - m1);
-  a = fmaf(DCG_L2, p2 - m2, a);
-  a = fmaf(DCG_L3, p3 - m3, a);
-  a = fmaf(DCG_L4, p4 - m4, a);
+// First derivative with pre-scaled weights w[0..3] (L_i / da).
+__device__ __forceinline__ float d1w(const float *w, float m1, float p1,
+                                     float m2, float p2, float m3, float p3,
+                                     float m4, float p4) {
+  float a = w[0] * (p1 - m1);
+  a = fmaf(w[1], p2 - m2, a);
+  a = fmaf(w[2], p3 - m3, a);
+  a = fmaf(w[3], p4 - m4, a);
   return a;
 }
 
@@ -93,7 +95,7 @@ constexpr float kCxy = 0.4546487134f, kCyz = 0.8414709848f;
 constexpr float kCxz = 0.5403023059f;
 constexpr float kV2pxFactor = 1.48f, kV2pnFactor = 1.2f;
 
-template <int TX, int TY, int NSTAGE, int MEDIUM, bool SPONGE>
+template <int TX, int TY, int MEDIUM, bool SPONGE>
 __global__ void __launch_bounds__(TX *TY, 1)
     fast_kernel(const __grid_constant__ CUtensorMap tm_pc,
                 const __grid_constant__ CUtensorMap tm_qc,
@@ -101,13 +103,15 @@ __global__ void __launch_bounds__(TX *TY, 1)
                 const __grid_constant__ CUtensorMap tm_qp,
                 const __grid_constant__ CUtensorMap tm_ca,
                 const __grid_constant__ CUtensorMap tm_cb,
-                const StepParams prm) {
+                const __grid_constant__ StepParams prm) {
+  constexpr int NSTAGE = 3;
   using Lay = FastLayout<TX, TY, NSTAGE, MEDIUM>;
   constexpr int HX = Lay::HX;
   constexpr int NT = Lay::NT;
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char *smem = reinterpret_cast<unsigned char *>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  // No static shared memory in this kernel: the dynamic window starts at
+  // the CTA's shared base, so this alignment holds and every access below
+  // is a shared-space access at a compile-time offset.
+  extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + Lay::OFF_BAR);
 
   const int tid = threadIdx.x;
@@ -121,6 +125,12 @@ __global__ void __launch_bounds__(TX *TY, 1)
   const bool active =
       gx >= prm.x0 && gx < prm.x1 && gy >= prm.y0 && gy < prm.y1;
 
+  // TMA destinations must be 128-byte aligned; refuse to run otherwise
+  // (CTA-uniform, before any copy is issued).
+  if (smem_u32(smem) & 127u) {
+    if (tid == 0) atomicOr(prm.err, kErrAlign);
+    return;
+  }
   if (tid == 0) {
     for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
     mbar_init_fence();
@@ -133,7 +143,7 @@ __global__ void __launch_bounds__(TX *TY, 1)
   }
   __syncthreads();
 
-  // Producer: one elected thread fills stage j % NSTAGE for iteration j.
+  // Producer: one elected thread fills stage j % 3 for iteration j.
   auto issue = [&](int j) {
     const int s = j % NSTAGE;
     unsigned char *st = smem + s * Lay::STAGE_BYTES;
@@ -168,23 +178,31 @@ __global__ void __launch_bounds__(TX *TY, 1)
   const float gxy = (SPONGE && active)
                         ? prm.sponge[gx] * prm.sponge[prm.sponge_oy + gy]
                         : 1.0f;
+  const bool src_col = active && gx == prm.src_x && gy == prm.src_y;
   const int c0 = (ty + kHalo) * HX + tx + kHalo;  // centre in a halo plane
   const int od = ty * HX + tx + kHalo;            // centre in a dy plane
   const int ot = ty * TX + tx;                    // centre in a tile
+  // global position of this column at the first output plane (advanced by
+  // one plane per output; never dereferenced for inactive threads)
+  const long long g0 = static_cast<long long>(zb) * prm.plane +
+                       static_cast<long long>(gy) * prm.pitch + gx;
+  float *out_p = prm.pp_out + g0;
+  float *out_q = prm.qp_out + g0;
 
-  for (int it0 = 0; it0 < n_it; it0 += 9) {
+  uint32_t mpar = 0;  // parity of the outer (9-plane) iteration
+  for (int it0 = 0; it0 < n_it; it0 += 9, mpar ^= 1u) {
 #pragma unroll
     for (int u = 0; u < 9; ++u) {
       const int it = it0 + u;
       if (it < n_it) {  // CTA-uniform
-        const int s = it % NSTAGE;
-        const uint32_t par = static_cast<uint32_t>(it / NSTAGE) & 1u;
-        unsigned char *st = smem + s * Lay::STAGE_BYTES;
-        const bool ok = mbar_wait_bounded(&bars[s], par, kWaitLimitNs);
+        // stage u % 3; its use count is it / 3 = 3 * (it0 / 9) + u / 3
+        unsigned char *st = smem + (u % 3) * Lay::STAGE_BYTES;
+        uint64_t *bar = &bars[u % 3];
+        const bool ok =
+            mbar_wait_bounded(bar, mpar ^ static_cast<uint32_t>((u / 3) & 1), kWaitLimitNs);
         const float *hp = reinterpret_cast<const float *>(st + Lay::OFF_HP);
         const float *hq = reinterpret_cast<const float *>(st + Lay::OFF_HQ);
-        float *dybp = reinterpret_cast<float *>(smem + Lay::OFF_DY +
-                                                (it & 1) * 2 * Lay::DY_BYTES);
+        float *dybp = reinterpret_cast<float *>(smem + Lay::OFF_DY + (u % 3) * 2 * Lay::DY_BYTES);
         float *dybq = dybp + Lay::DY_BYTES / 4;
 
         // ---- leading plane k: centre, x/y second and first derivatives
@@ -199,11 +217,11 @@ __global__ void __launch_bounds__(TX *TY, 1)
                       ym2 = h[c0 - 2 * HX], yp2 = h[c0 + 2 * HX],
                       ym3 = h[c0 - 3 * HX], yp3 = h[c0 + 3 * HX],
                       ym4 = h[c0 - 4 * HX], yp4 = h[c0 + 4 * HX];
-          pxx = d2w(c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4) * prm.dxxinv;
-          pyy = d2w(c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4) * prm.dyyinv;
+          pxx = d2w(prm.w2x, c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
+          pyy = d2w(prm.w2y, c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
           cqp[u] = c;
-          dxp[u] = d1w(xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
-          dyp[u] = d1w(ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
+          dxp[u] = d1w(prm.w1x, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
+          dyp[u] = d1w(prm.w1y, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
           dybp[od] = dyp[u];
         }
         {
@@ -216,11 +234,11 @@ __global__ void __launch_bounds__(TX *TY, 1)
                       ym2 = h[c0 - 2 * HX], yp2 = h[c0 + 2 * HX],
                       ym3 = h[c0 - 3 * HX], yp3 = h[c0 + 3 * HX],
                       ym4 = h[c0 - 4 * HX], yp4 = h[c0 + 4 * HX];
-          qxx = d2w(c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4) * prm.dxxinv;
-          qyy = d2w(c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4) * prm.dyyinv;
+          qxx = d2w(prm.w2x, c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
+          qyy = d2w(prm.w2y, c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
           cqq[u] = c;
-          dxq[u] = d1w(xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
-          dyq[u] = d1w(ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
+          dxq[u] = d1w(prm.w1x, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
+          dyq[u] = d1w(prm.w1y, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
           dybq[od] = dyq[u];
         }
         // y-derivatives of the 4 + 4 halo columns (needed by d2/dxdy)
@@ -229,31 +247,27 @@ __global__ void __launch_bounds__(TX *TY, 1)
           const int hx = hc < 4 ? hc : TX + hc;
           const int o = (hy + kHalo) * HX + hx;
           dybp[hy * HX + hx] =
-              d1w(hp[o - HX], hp[o + HX], hp[o - 2 * HX], hp[o + 2 * HX],
-                  hp[o - 3 * HX], hp[o + 3 * HX], hp[o - 4 * HX],
-                  hp[o + 4 * HX]);
+              d1w(prm.w1y, hp[o - HX], hp[o + HX], hp[o - 2 * HX], hp[o + 2 * HX],
+                  hp[o - 3 * HX], hp[o + 3 * HX], hp[o - 4 * HX], hp[o + 4 * HX]);
           dybq[hy * HX + hx] =
-              d1w(hq[o - HX], hq[o + HX], hq[o - 2 * HX], hq[o + 2 * HX],
-                  hq[o - 3 * HX], hq[o + 3 * HX], hq[o - 4 * HX],
-                  hq[o + 4 * HX]);
+              d1w(prm.w1y, hq[o - HX], hq[o + HX], hq[o - 2 * HX], hq[o + 2 * HX],
+                  hq[o - 3 * HX], hq[o + 3 * HX], hq[o - 4 * HX], hq[o + 4 * HX]);
         }
         if (__syncthreads_or(!ok)) {
           abort_it = it;
           goto done;
         }
-        // The slot read in iteration it-1 is free: refill it.
+        // The stage read in iteration it-1 is free: refill it.
         if (tid == 0 && it + NSTAGE - 1 < n_it) issue(it + NSTAGE - 1);
 
         // ---- in-plane part of H1/H2 at plane k, delayed to output time
         if (it >= kHalo && it < n_it - kHalo) {
-          const float pxy = d1w(dybp[od - 1], dybp[od + 1], dybp[od - 2],
+          const float pxy = d1w(prm.w1x, dybp[od - 1], dybp[od + 1], dybp[od - 2],
                                 dybp[od + 2], dybp[od - 3], dybp[od + 3],
-                                dybp[od - 4], dybp[od + 4]) *
-                            prm.dxyinv;
-          const float qxy = d1w(dybq[od - 1], dybq[od + 1], dybq[od - 2],
+                                dybp[od - 4], dybp[od + 4]);
+          const float qxy = d1w(prm.w1x, dybq[od - 1], dybq[od + 1], dybq[od - 2],
                                 dybq[od + 2], dybq[od - 3], dybq[od + 3],
-                                dybq[od - 4], dybq[od + 4]) *
-                            prm.dxyinv;
+                                dybq[od - 4], dybq[od + 4]);
           float cxx, cyy, cxy;
           if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) {
             const float *ca = reinterpret_cast<const float *>(st + Lay::OFF_CA);
@@ -273,29 +287,22 @@ __global__ void __launch_bounds__(TX *TY, 1)
 
         // ---- output plane z = k - 4
         if (it >= 2 * kHalo) {
-          const int z = zb + it - 2 * kHalo;
           // ring slots of planes z-4 .. z+4 (u is a compile-time constant)
           const int m4 = (u + 1) % 9, m3 = (u + 2) % 9, m2 = (u + 3) % 9,
                     m1 = (u + 4) % 9, c = (u + 5) % 9, p1 = (u + 6) % 9,
                     p2 = (u + 7) % 9, p3 = (u + 8) % 9, p4 = u;
-          const float pzz = d2w(cqp[c], cqp[m1], cqp[p1], cqp[m2], cqp[p2],
-                                cqp[m3], cqp[p3], cqp[m4], cqp[p4]) *
-                            prm.dzzinv;
-          const float qzz = d2w(cqq[c], cqq[m1], cqq[p1], cqq[m2], cqq[p2],
-                                cqq[m3], cqq[p3], cqq[m4], cqq[p4]) *
-                            prm.dzzinv;
-          const float pxz = d1w(dxp[m1], dxp[p1], dxp[m2], dxp[p2], dxp[m3],
-                                dxp[p3], dxp[m4], dxp[p4]) *
-                            prm.dxzinv;
-          const float qxz = d1w(dxq[m1], dxq[p1], dxq[m2], dxq[p2], dxq[m3],
-                                dxq[p3], dxq[m4], dxq[p4]) *
-                            prm.dxzinv;
-          const float pyz = d1w(dyp[m1], dyp[p1], dyp[m2], dyp[p2], dyp[m3],
-                                dyp[p3], dyp[m4], dyp[p4]) *
-                            prm.dyzinv;
-          const float qyz = d1w(dyq[m1], dyq[p1], dyq[m2], dyq[p2], dyq[m3],
-                                dyq[p3], dyq[m4], dyq[p4]) *
-                            prm.dyzinv;
+          const float pzz = d2w(prm.w2z, cqp[c], cqp[m1], cqp[p1], cqp[m2], cqp[p2],
+                                cqp[m3], cqp[p3], cqp[m4], cqp[p4]);
+          const float qzz = d2w(prm.w2z, cqq[c], cqq[m1], cqq[p1], cqq[m2], cqq[p2],
+                                cqq[m3], cqq[p3], cqq[m4], cqq[p4]);
+          const float pxz = d1w(prm.w1z, dxp[m1], dxp[p1], dxp[m2], dxp[p2], dxp[m3],
+                                dxp[p3], dxp[m4], dxp[p4]);
+          const float qxz = d1w(prm.w1z, dxq[m1], dxq[p1], dxq[m2], dxq[p2], dxq[m3],
+                                dxq[p3], dxq[m4], dxq[p4]);
+          const float pyz = d1w(prm.w1z, dyp[m1], dyp[p1], dyp[m2], dyp[p2], dyp[m3],
+                                dyp[p3], dyp[m4], dyp[p4]);
+          const float qyz = d1w(prm.w1z, dyq[m1], dyq[p1], dyq[m2], dyq[p2], dyq[m3],
+                                dyq[p3], dyq[m4], dyq[p4]);
           const float *cb = reinterpret_cast<const float *>(st + Lay::OFF_CB);
           const float *own = reinterpret_cast<const float *>(st + Lay::OFF_OWN);
           float czz, cxz, cyz, v2px, v2pz, v2sz, v2pn;
@@ -321,13 +328,12 @@ __global__ void __launch_bounds__(TX *TY, 1)
           const float h2p = bp[c] + pzz - h1p;
           const float h1q = fmaf(cyz, qyz, fmaf(cxz, qxz, fmaf(czz, qzz, aq[c])));
           const float h2q = bq[c] + qzz - h1q;
-          const float rhsp =
-              fmaf(v2sz, h1p - h1q, fmaf(v2pz, h1q, v2px * h2p));
-          const float rhsq =
-              fmaf(-v2sz, h2p - h2q, fmaf(v2pz, h1q, v2pn * h2p));
+          const float rhsp = fmaf(v2sz, h1p - h1q, fmaf(v2pz, h1q, v2px * h2p));
+          const float rhsq = fmaf(-v2sz, h2p - h2q, fmaf(v2pz, h1q, v2pn * h2p));
           const float ppo = own[ot], qpo = own[NT + ot];
           float np, nq;
           if (SPONGE) {
+            const int z = zb + it - 2 * kHalo;
             const float g = gxy * prm.sponge[prm.sponge_oz + z];
             np = fmaf(rhsp, prm.dt2, fmaf(-g, ppo, 2.0f * cqp[c])) * g;
             nq = fmaf(rhsq, prm.dt2, fmaf(-g, qpo, 2.0f * cqq[c])) * g;
@@ -336,10 +342,8 @@ __global__ void __launch_bounds__(TX *TY, 1)
             nq = fmaf(rhsq, prm.dt2, 2.0f * cqq[c] - qpo);
           }
           if (active) {
-            const long long gi = static_cast<long long>(z) * prm.plane +
-                                 static_cast<long long>(gy) * prm.pitch + gx;
             if (prm.energy) e_acc = fmaf(np, np, fmaf(nq, nq, e_acc));
-            if (gx == prm.src_x && gy == prm.src_y && z == prm.src_z) {
+            if (src_col && zb + it - 2 * kHalo == prm.src_z) {
               const int step = *prm.d_step + prm.step_offset;
               const float sv =
                   step + 1 < prm.src_count ? prm.src_table[step + 1] : 0.0f;
@@ -348,9 +352,11 @@ __global__ void __launch_bounds__(TX *TY, 1)
               np += sv;
               nq += sv;
             }
-            prm.pp_out[gi] = np;
-            prm.qp_out[gi] = nq;
+            *out_p = np;
+            *out_q = nq;
           }
+          out_p += prm.plane;
+          out_q += prm.plane;
         }
       }
     }
@@ -387,14 +393,14 @@ done:
 }
 
 // Compiled tile shape.  TX = 32 (one warp per tile row), TY = 16 rows,
-// a 4-stage TMA ring; see the design doc for the choice.
-constexpr int kTX = 32, kTY = 16, kStages = 4;
+// a 3-stage TMA ring.
+constexpr int kTX = 32, kTY = 16, kStages = 3;
 
 template <int MEDIUM, bool SPONGE>
 cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int pc_buf,
                           int qc_buf, int pp_buf, int qp_buf) {
   using Lay = FastLayout<kTX, kTY, kStages, MEDIUM>;
-  auto kern = fast_kernel<kTX, kTY, kStages, MEDIUM, SPONGE>;
+  auto kern = fast_kernel<kTX, kTY, MEDIUM, SPONGE>;
   const int nx = prm.x1 - prm.tile_x0, ny = prm.y1 - prm.tile_y0;
   const int nz = prm.z1 - prm.z0;
   dim3 grid((nx + kTX - 1) / kTX, (ny + kTY - 1) / kTY,
@@ -409,7 +415,7 @@ cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int pc_buf,
 template <int MEDIUM, bool SPONGE>
 cudaError_t set_smem_attr() {
   using Lay = FastLayout<kTX, kTY, kStages, MEDIUM>;
-  return cudaFuncSetAttribute(fast_kernel<kTX, kTY, kStages, MEDIUM, SPONGE>,
+  return cudaFuncSetAttribute(fast_kernel<kTX, kTY, MEDIUM, SPONGE>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM_BYTES);
 }
 
