@@ -3,6 +3,7 @@
 // medium generator; plus tensor-map encoding.
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -12,22 +13,26 @@
 namespace dcg {
 namespace {
 
-__global__ void add_source_kernel(float *pc, float *qc, long long gi,
-                                  const float *table, int count,
-                                  const int *d_step, int step_offset) {
+__global__ void add_source_kernel(float2 *cur, long long gi, const float *table,
+                                  int count, const int *d_step,
+                                  int step_offset) {
   // src/device_data.cu:131-139 with the amplitude looked up on the device
   const int step = *d_step + step_offset;
   const float s = (step >= 0 && step < count) ? table[step] : 0.0f;
-  pc[gi] = __fadd_rn(pc[gi], s);
-  qc[gi] = __fadd_rn(qc[gi], s);
+  float2 v = cur[gi];
+  v.x = __fadd_rn(v.x, s);
+  v.y = __fadd_rn(v.y, s);
+  cur[gi] = v;
 }
 
-__global__ void add_value_kernel(float *pc, float *qc, long long gi, float s) {
-  pc[gi] = __fadd_rn(pc[gi], s);
-  qc[gi] = __fadd_rn(qc[gi], s);
+__global__ void add_value_kernel(float2 *cur, long long gi, float s) {
+  float2 v = cur[gi];
+  v.x = __fadd_rn(v.x, s);
+  v.y = __fadd_rn(v.y, s);
+  cur[gi] = v;
 }
 
-__global__ void gather_kernel(const float *p, const long long *idx, int n,
+__global__ void gather_kernel(const float2 *f, const long long *idx, int n,
                               float *traces, int cap, const int *d_step,
                               int step_offset, long long src_gi,
                               const float *src_pre) {
@@ -38,7 +43,43 @@ __global__ void gather_kernel(const float *p, const long long *idx, int n,
   // the source point already holds the next step's source: record the value
   // the stencil produced, as the reference sees it after the swap
   traces[static_cast<long long>(step) * n + r] =
-      (i == src_gi && src_pre) ? src_pre[0] : p[i];
+      (i == src_gi && src_pre) ? src_pre[0] : f[i].x;
+}
+
+__global__ void pack_kernel(float2 *dst, const float *p, const float *q,
+                            long long sx, long long sy, long long n,
+                            long long pitch) {
+  for (long long d = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; d < n;
+       d += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long x = d % sx, yz = d / sx;
+    dst[yz * pitch + x] = make_float2(p ? p[d] : 0.0f, q ? q[d] : 0.0f);
+  }
+}
+
+__global__ void unpack_kernel(const float2 *src, float *p, float *q, long long sx,
+                              long long sy, long long n, long long pitch) {
+  for (long long d = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; d < n;
+       d += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long x = d % sx, yz = d / sx;
+    const float2 v = src[yz * pitch + x];
+    if (p) p[d] = v.x;
+    if (q) q[d] = v.y;
+  }
+}
+
+__global__ void box_copy_kernel(float2 *pairs, int comp, float *dense, long long bx,
+                                long long by, long long bz, long long wx, long long wy,
+                                long long n, long long pitch, long long plane,
+                                bool to_dense) {
+  for (long long d = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; d < n;
+       d += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long x = d % wx, y = (d / wx) % wy, z = d / (wx * wy);
+    float *e = reinterpret_cast<float *>(pairs + (bz + z) * plane + (by + y) * pitch + bx + x) + comp;
+    if (to_dense)
+      dense[d] = *e;
+    else
+      *e = dense[d];
+  }
 }
 
 __global__ void advance_kernel(int *d_step, int by) { *d_step += by; }
@@ -138,25 +179,54 @@ __global__ void layered_kernel(const dc_gb300_layered_spec spec_v, float *coef,
 
 }  // namespace
 
-cudaError_t launch_add_source(cudaStream_t st, float *pc, float *qc,
-                              long long gi, const float *table, int count,
-                              const int *d_step, int step_offset) {
-  add_source_kernel<<<1, 1, 0, st>>>(pc, qc, gi, table, count, d_step, step_offset);
+cudaError_t launch_add_source(cudaStream_t st, float2 *cur, long long gi,
+                              const float *table, int count, const int *d_step,
+                              int step_offset) {
+  add_source_kernel<<<1, 1, 0, st>>>(cur, gi, table, count, d_step, step_offset);
   return cudaGetLastError();
 }
 
-cudaError_t launch_add_value(cudaStream_t st, float *pc, float *qc,
-                             long long gi, float value) {
-  add_value_kernel<<<1, 1, 0, st>>>(pc, qc, gi, value);
+cudaError_t launch_add_value(cudaStream_t st, float2 *cur, long long gi, float value) {
+  add_value_kernel<<<1, 1, 0, st>>>(cur, gi, value);
   return cudaGetLastError();
 }
 
-cudaError_t launch_gather(cudaStream_t st, const float *p,
-                          const long long *idx, int n, float *traces, int cap,
-                          const int *d_step, int step_offset,
+cudaError_t launch_gather(cudaStream_t st, const float2 *f, const long long *idx, int n,
+                          float *traces, int cap, const int *d_step, int step_offset,
                           long long src_gi, const float *src_pre) {
-  gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(p, idx, n, traces, cap, d_step,
+  gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(f, idx, n, traces, cap, d_step,
                                                  step_offset, src_gi, src_pre);
+  return cudaGetLastError();
+}
+
+namespace {
+int grid_for(long long n) {
+  return static_cast<int>(std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 32)));
+}
+}  // namespace
+
+cudaError_t launch_pack(cudaStream_t st, float2 *dst, const float *p, const float *q,
+                        long long sx, long long sy, long long sz, long long pitch) {
+  const long long n = sx * sy * sz;
+  pack_kernel<<<grid_for(n), 256, 0, st>>>(dst, p, q, sx, sy, n, pitch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(cudaStream_t st, const float2 *src, float *p, float *q,
+                          long long sx, long long sy, long long sz, long long pitch) {
+  const long long n = sx * sy * sz;
+  unpack_kernel<<<grid_for(n), 256, 0, st>>>(src, p, q, sx, sy, n, pitch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_box_copy(cudaStream_t st, float2 *pairs, int comp, float *dense,
+                            const long long b0[3], const long long b1[3], long long pitch,
+                            long long plane, bool to_dense) {
+  const long long wx = b1[0] - b0[0], wy = b1[1] - b0[1], wz = b1[2] - b0[2];
+  const long long n = wx * wy * wz;
+  if (n <= 0) return cudaSuccess;
+  box_copy_kernel<<<grid_for(n), 256, 0, st>>>(pairs, comp, dense, b0[0], b0[1], b0[2], wx, wy,
+                                               n, pitch, plane, to_dense);
   return cudaGetLastError();
 }
 
@@ -186,7 +256,7 @@ cudaError_t launch_layered(cudaStream_t st, const dc_gb300_layered_spec &spec,
 
 bool encode_tiled(CUtensorMap *map, const void *base, int rank,
                   const uint64_t *dims, const uint64_t *strides_bytes,
-                  const uint32_t *box, std::string *err) {
+                  const uint32_t *box, std::string *err, bool pairs) {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
   static cudaError_t lookup_err = cudaSuccess;
@@ -203,7 +273,10 @@ bool encode_tiled(CUtensorMap *map, const void *base, int rank,
     return false;
   }
   cuuint32_t elem_strides[5] = {1, 1, 1, 1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, const_cast<void *>(base),
+  // (p, q) pairs travel as opaque 8-byte elements
+  const CUtensorMapDataType dt =
+      pairs ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  CUresult r = fn(map, dt, rank, const_cast<void *>(base),
                   dims, strides_bytes, box, elem_strides, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);

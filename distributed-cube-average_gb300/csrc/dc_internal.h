@@ -53,9 +53,12 @@ struct StepParams {
   // fast kernel: FD weights pre-scaled by the grid spacing
   float w2x[5], w2y[5], w2z[5];  // K_i / da^2 (second derivative)
   float w1x[4], w1y[4], w1z[4];  // L_i / da   (first derivative, i = 1..4)
+  float n1x[4], n1y[4], n1z[4];  // -L_i / da
   float dt, dt2;
-  float *pp_out, *qp_out;       // pp/qp buffers (read, then written in place)
-  const float *pc_in, *qc_in;   // current fields (exact kernel reads these)
+  // Wavefields are stored as interleaved (p, q) pairs: `prev` holds
+  // (pp, qp) and is updated in place, `cur` holds (pc, qc).
+  float2 *prev;
+  const float2 *cur;
   const float *coef;            // [DC_NCOEF][count]
   const float *vv;              // [2][count]: vpz, vsv (VPZ_VSV medium)
   long long count;              // floats per array (incl. pitch padding)
@@ -83,7 +86,9 @@ struct Sim {
   float dx = 0, dy = 0, dz = 0, dt = 0;
   int kernel = DC_GB300_KERNEL_FAST;
   int medium = DC_GB300_MEDIUM_PRECOMP;
-  float *field[4] = {nullptr, nullptr, nullptr, nullptr};
+  // two pair buffers of `count` (p, q) elements; which one is "previous"
+  // and which "current" is read from the reference-ABI view (abi.pp/abi.pc)
+  float2 *pq[2] = {nullptr, nullptr};
   float *coef = nullptr;       // [DC_NCOEF][count]
   float *vv = nullptr;         // [2][count]
   float *sponge = nullptr;     // [sx + sy + sz]
@@ -110,7 +115,7 @@ struct Sim {
   long long launches = 0;
   int config_version = 0;
   // tensor maps for the fast kernel (encoded for one tile shape)
-  CUtensorMap tm_halo[4], tm_own[4], tm_ca, tm_cb;
+  CUtensorMap tm_halo[2], tm_own[2], tm_ca, tm_cb;
   int maps_tx = 0, maps_ty = 0;
   // captured multi-step graphs, keyed by start parity of the pc buffer
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -127,18 +132,31 @@ FastShape fast_shape(const Sim *sim);
 bool fast_encode_maps(Sim *sim, std::string *err);
 
 // Launchers.  Return the cudaError_t of the launch.
-cudaError_t launch_fast(Sim *sim, const StepParams &prm, int pc_buf,
-                        int qc_buf, int pp_buf, int qp_buf);
+cudaError_t launch_fast(Sim *sim, const StepParams &prm, int cur_buf,
+                        int prev_buf);
 cudaError_t launch_exact(Sim *sim, const StepParams &prm);
-cudaError_t launch_add_source(cudaStream_t st, float *pc, float *qc,
-                              long long gi, const float *table, int count,
+cudaError_t launch_add_source(cudaStream_t st, float2 *cur, long long gi,
+                              const float *table, int count,
                               const int *d_step, int step_offset);
-cudaError_t launch_add_value(cudaStream_t st, float *pc, float *qc,
-                             long long gi, float value);
-cudaError_t launch_gather(cudaStream_t st, const float *p,
+cudaError_t launch_add_value(cudaStream_t st, float2 *cur, long long gi,
+                             float value);
+cudaError_t launch_gather(cudaStream_t st, const float2 *f,
                           const long long *idx, int n, float *traces, int cap,
                           const int *d_step, int step_offset,
                           long long src_gi, const float *src_pre);
+// Dense (x fastest, no pitch) p and q arrays <-> pitched pair buffer; a null
+// dense pointer reads as zeros / is skipped.
+cudaError_t launch_pack(cudaStream_t st, float2 *dst, const float *p,
+                        const float *q, long long sx, long long sy,
+                        long long sz, long long pitch);
+cudaError_t launch_unpack(cudaStream_t st, const float2 *src, float *p,
+                          float *q, long long sx, long long sy, long long sz,
+                          long long pitch);
+// One component (0 = p, 1 = q) of a box of a pair buffer <-> dense buffer.
+cudaError_t launch_box_copy(cudaStream_t st, float2 *pairs, int comp,
+                            float *dense, const long long b0[3],
+                            const long long b1[3], long long pitch,
+                            long long plane, bool to_dense);
 cudaError_t launch_advance_step(cudaStream_t st, int *d_step, int by);
 cudaError_t launch_precomp(cudaStream_t st, const float *theta,
                            const float *phi, const float *vsv,
@@ -152,7 +170,8 @@ cudaError_t launch_layered(cudaStream_t st, const dc_gb300_layered_spec &spec,
 // Tensor-map encoding through the driver entry point (no -lcuda needed).
 bool encode_tiled(CUtensorMap *map, const void *base, int rank,
                   const uint64_t *dims, const uint64_t *strides_bytes,
-                  const uint32_t *box, std::string *err);
+                  const uint32_t *box, std::string *err,
+                  bool pairs = false);
 
 // Thread-local error text for dc_gb300_last_error().
 void set_error(const std::string &msg);

@@ -52,10 +52,35 @@ cudaError_t download_dense(Sim *s, float *dst, const float *src) {
                            s->sy * s->sz, cudaMemcpyDeviceToHost, s->stream);
 }
 
-int buffer_of(const Sim *s, const float *p) {
-  for (int b = 0; b < 4; ++b)
-    if (s->field[b] == p) return b;
+// Pair buffer that holds the field whose p component is `p` and q component
+// `q` (q == p + 1), or -1.
+int pair_of(const Sim *s, const float *p, const float *q) {
+  for (int b = 0; b < 2; ++b) {
+    const float *base = reinterpret_cast<const float *>(s->pq[b]);
+    if (p == base && q == base + 1) return b;
+  }
   return -1;
+}
+
+// Pair buffer and component (0 = p, 1 = q) of a field pointer, or -1.
+int component_of(const Sim *s, const float *f, int *comp) {
+  for (int b = 0; b < 2; ++b) {
+    const float *base = reinterpret_cast<const float *>(s->pq[b]);
+    if (f == base || f == base + 1) {
+      *comp = static_cast<int>(f - base);
+      return b;
+    }
+  }
+  return -1;
+}
+
+// Buffers of the current and previous fields, or false when the ABI view
+// has been rearranged into something the kernels cannot address.
+bool roles(const Sim *s, int *cur, int *prev) {
+  const dc_device_data &a = s->handle->abi;
+  *cur = pair_of(s, a.pc, a.qc);
+  *prev = pair_of(s, a.pp, a.qp);
+  return *cur >= 0 && *prev >= 0 && *cur != *prev;
 }
 
 // Keeps the reference-ABI view in step with the device arrays.
@@ -89,7 +114,7 @@ void release(Sim *s) {
   if (!s) return;
   if (s->stream) cudaStreamSynchronize(s->stream);
   drop_graphs(s);
-  for (float *&f : s->field) {
+  for (float2 *&f : s->pq) {
     cudaFree(f);
     f = nullptr;
   }
@@ -141,15 +166,16 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
       p.w1x[k] = static_cast<float>(L[k] / hx);
       p.w1y[k] = static_cast<float>(L[k] / hy);
       p.w1z[k] = static_cast<float>(L[k] / hz);
+      p.n1x[k] = -p.w1x[k];
+      p.n1y[k] = -p.w1y[k];
+      p.n1z[k] = -p.w1z[k];
     }
   }
   p.dt = dt;
   p.dt2 = dt * dt;
   const dc_device_data &a = s->handle->abi;
-  p.pp_out = a.pp;
-  p.qp_out = a.qp;
-  p.pc_in = a.pc;
-  p.qc_in = a.qc;
+  p.prev = reinterpret_cast<float2 *>(a.pp);
+  p.cur = reinterpret_cast<const float2 *>(a.pc);
   p.coef = s->coef;
   p.vv = s->vv;
   p.count = s->count;
@@ -166,9 +192,9 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
 cudaError_t launch_pass(Sim *s, const StepParams &p) {
   ++s->launches;
   if (s->kernel == DC_GB300_KERNEL_EXACT) return launch_exact(s, p);
-  const dc_device_data &a = s->handle->abi;
-  return launch_fast(s, p, buffer_of(s, a.pc), buffer_of(s, a.qc),
-                     buffer_of(s, a.pp), buffer_of(s, a.qp));
+  int cur = -1, prev = -1;
+  roles(s, &cur, &prev);  // checked by the callers
+  return launch_fast(s, p, cur, prev);
 }
 
 void swap_roles(dc_device_data *a) {
@@ -202,7 +228,8 @@ cudaError_t queue_step(Sim *s, int j) {
   if (s->nrec > 0) {
     ++s->launches;
     const long long src_gi = s->src_gi;
-    e = launch_gather(s->stream, s->handle->abi.pp, s->d_rec, s->nrec,
+    e = launch_gather(s->stream, reinterpret_cast<const float2 *>(s->handle->abi.pp), s->d_rec,
+                      s->nrec,
                       s->d_traces, s->trace_cap, s->d_step, j, src_gi,
                       s->d_src_pre);
     if (e != cudaSuccess) return e;
@@ -300,8 +327,8 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamDefault) != cudaSuccess)
     return bail(fail(DC_GB300_ERR_CUDA, "cudaStreamCreate failed"));
   const size_t bytes = static_cast<size_t>(s->count) * 4;
-  for (int b = 0; b < 4; ++b)
-    if (cudaMalloc(&s->field[b], bytes) != cudaSuccess)
+  for (int b = 0; b < 2; ++b)
+    if (cudaMalloc(&s->pq[b], bytes * 2) != cudaSuccess)
       return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of a wavefield failed"));
   if (s->medium == DC_GB300_MEDIUM_PRECOMP) {
     if (cudaMalloc(&s->coef, bytes * DC_NCOEF) != cudaSuccess)
@@ -314,8 +341,8 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
       cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&s->d_src_pre, 2 * sizeof(float)) != cudaSuccess)
     return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of counters failed"));
-  for (int b = 0; b < 4; ++b)
-    if (cudaMemsetAsync(s->field[b], 0, bytes, s->stream) != cudaSuccess)
+  for (int b = 0; b < 2; ++b)
+    if (cudaMemsetAsync(s->pq[b], 0, bytes * 2, s->stream) != cudaSuccess)
       return bail(fail(DC_GB300_ERR_CUDA, "cudaMemset failed"));
   if (s->coef) cudaMemsetAsync(s->coef, 0, bytes * DC_NCOEF, s->stream);
   if (s->vv) cudaMemsetAsync(s->vv, 0, bytes * 2, s->stream);
@@ -325,10 +352,12 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
   std::string err;
   if (s->kernel == DC_GB300_KERNEL_FAST && !fast_encode_maps(s, &err))
     return bail(fail(DC_GB300_ERR_CUDA, err));
-  h->abi.pp = s->field[0];
-  h->abi.pc = s->field[1];
-  h->abi.qp = s->field[2];
-  h->abi.qc = s->field[3];
+  // (pp, qp) live in pair buffer 0 and (pc, qc) in pair buffer 1; the q
+  // pointer is the p pointer + 1 (interleaved storage)
+  h->abi.pp = reinterpret_cast<float *>(s->pq[0]);
+  h->abi.qp = h->abi.pp + 1;
+  h->abi.pc = reinterpret_cast<float *>(s->pq[1]);
+  h->abi.qc = h->abi.pc + 1;
   refresh_abi(s);
   if (cudaStreamSynchronize(s->stream) != cudaSuccess)
     return bail(fail(DC_GB300_ERR_CUDA, "initialisation failed"));
@@ -489,16 +518,30 @@ extern "C" int dc_gb300_set_fields(dc_gb300_sim *h, const float *pp, const float
   Sim *s = impl(h);
   if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
   DCG_TRY(cudaSetDevice(s->device));
-  dc_device_data &a = h->abi;
-  float *dst[4] = {a.pp, a.pc, a.qp, a.qc};
-  const float *src[4] = {pp, pc, qp, qc};
-  for (int k = 0; k < 4; ++k) {
-    if (src[k]) {
-      DCG_TRY(upload_dense(s, dst[k], src[k]));
-    } else {
-      DCG_TRY(cudaMemsetAsync(dst[k], 0, static_cast<size_t>(s->count) * 4, s->stream));
+  int cur = -1, prev = -1;
+  if (!roles(s, &cur, &prev)) return fail(DC_GB300_ERR_STATE, "field pointers rearranged");
+  const long long n = s->sx * s->sy * s->sz;
+  float *stage = nullptr;
+  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
+  const float *src[2][2] = {{pp, qp}, {pc, qc}};
+  const int dst[2] = {prev, cur};
+  for (int k = 0; k < 2; ++k) {
+    const float *dp = nullptr, *dq = nullptr;
+    if (src[k][0]) {
+      DCG_TRY(cudaMemcpyAsync(stage, src[k][0], sizeof(float) * n, cudaMemcpyHostToDevice,
+                              s->stream));
+      dp = stage;
     }
+    if (src[k][1]) {
+      DCG_TRY(cudaMemcpyAsync(stage + n, src[k][1], sizeof(float) * n, cudaMemcpyHostToDevice,
+                              s->stream));
+      dq = stage + n;
+    }
+    // the pitch padding stays zero: clear, then pack the dense arrays
+    DCG_TRY(cudaMemsetAsync(s->pq[dst[k]], 0, sizeof(float2) * s->count, s->stream));
+    DCG_TRY(launch_pack(s->stream, s->pq[dst[k]], dp, dq, s->sx, s->sy, s->sz, s->pitch));
   }
+  DCG_TRY(cudaFreeAsync(stage, s->stream));
   DCG_TRY(cudaMemsetAsync(s->d_step, 0, sizeof(int), s->stream));
   if (s->d_energy) DCG_TRY(cudaMemsetAsync(s->d_energy, 0, sizeof(double) * s->energy_cap, s->stream));
   if (s->d_traces)
@@ -514,11 +557,25 @@ extern "C" int dc_gb300_get_fields(dc_gb300_sim *h, float *pp, float *pc, float 
   Sim *s = impl(h);
   if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
   DCG_TRY(cudaSetDevice(s->device));
-  dc_device_data &a = h->abi;
-  float *dst[4] = {pp, pc, qp, qc};
-  const float *src[4] = {a.pp, a.pc, a.qp, a.qc};
-  for (int k = 0; k < 4; ++k)
-    if (dst[k]) DCG_TRY(download_dense(s, dst[k], src[k]));
+  int cur = -1, prev = -1;
+  if (!roles(s, &cur, &prev)) return fail(DC_GB300_ERR_STATE, "field pointers rearranged");
+  const long long n = s->sx * s->sy * s->sz;
+  float *stage = nullptr;
+  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
+  float *dst[2][2] = {{pp, qp}, {pc, qc}};
+  const int src[2] = {prev, cur};
+  for (int k = 0; k < 2; ++k) {
+    if (!dst[k][0] && !dst[k][1]) continue;
+    DCG_TRY(launch_unpack(s->stream, s->pq[src[k]], stage, stage + n, s->sx, s->sy, s->sz,
+                          s->pitch));
+    if (dst[k][0])
+      DCG_TRY(cudaMemcpyAsync(dst[k][0], stage, sizeof(float) * n, cudaMemcpyDeviceToHost,
+                              s->stream));
+    if (dst[k][1])
+      DCG_TRY(cudaMemcpyAsync(dst[k][1], stage + n, sizeof(float) * n, cudaMemcpyDeviceToHost,
+                              s->stream));
+  }
+  DCG_TRY(cudaFreeAsync(stage, s->stream));
   DCG_TRY(cudaStreamSynchronize(s->stream));
   return DC_GB300_OK;
 }
@@ -692,6 +749,8 @@ extern "C" int dc_gb300_run(dc_gb300_sim *h, int steps) {
   if (steps < 0) return fail(DC_GB300_ERR_ARG, "negative step count");
   if (steps == 0) return DC_GB300_OK;
   DCG_TRY(cudaSetDevice(s->device));
+  int cur0 = -1, prev0 = -1;
+  if (!roles(s, &cur0, &prev0)) return fail(DC_GB300_ERR_STATE, "field pointers rearranged");
   if (s->energy_cap > 0 && s->steps_done + steps > s->energy_cap)
     return fail(DC_GB300_ERR_ARG, "run exceeds the energy capacity");
   if (s->nrec > 0 && s->steps_done + steps > s->trace_cap)
@@ -700,21 +759,22 @@ extern "C" int dc_gb300_run(dc_gb300_sim *h, int steps) {
   // (src/worker.c:467-470); later ones are fused into the previous store.
   if (s->src_gi >= 0 && s->src_applied_step != s->steps_done) {
     ++s->launches;
-    DCG_TRY(launch_add_source(s->stream, h->abi.pc, h->abi.qc, s->src_gi, s->d_src,
-                              s->src_count, s->d_step, 0));
+    DCG_TRY(launch_add_source(s->stream, reinterpret_cast<float2 *>(h->abi.pc), s->src_gi,
+                              s->d_src, s->src_count, s->d_step, 0));
   }
   int left = steps;
   while (left >= kGraphChunk) {
-    const int par = buffer_of(s, h->abi.pc) & 1;  // pc is buffer 1 or 0
-    const int slot = par;
+    int cur = -1, prev = -1;
+    roles(s, &cur, &prev);
+    const int slot = cur;  // graphs are keyed by the buffer holding pc
     if (!s->graph[slot] || s->graph_version[slot] != s->config_version ||
-        s->graph_pc[slot] != buffer_of(s, h->abi.pc)) {
+        s->graph_pc[slot] != cur) {
       if (s->graph[slot]) cudaGraphExecDestroy(s->graph[slot]);
       s->graph[slot] = nullptr;
       int rc = capture_chunk(s, &s->graph[slot]);
       if (rc != DC_GB300_OK) return rc;
       s->graph_version[slot] = s->config_version;
-      s->graph_pc[slot] = buffer_of(s, h->abi.pc);
+      s->graph_pc[slot] = cur;
     }
     DCG_TRY(cudaGraphLaunch(s->graph[slot], s->stream));
     s->launches += kGraphChunk * launches_per_step(s) + 1;
@@ -753,9 +813,8 @@ extern "C" int dc_gb300_propagate_box(dc_gb300_sim *h, const size_t start[3],
     if (b0[d] < 4 || b1[d] > lim[d] - 4)
       return fail(DC_GB300_ERR_ARG, "box outside the updatable region [4, size-4)");
   }
-  const dc_device_data &a = h->abi;
-  if (buffer_of(s, a.pp) < 0 || buffer_of(s, a.pc) < 0 || buffer_of(s, a.qp) < 0 ||
-      buffer_of(s, a.qc) < 0)
+  int cur = -1, prev = -1;
+  if (!roles(s, &cur, &prev))
     return fail(DC_GB300_ERR_STATE, "field pointers do not belong to this simulation");
   DCG_TRY(cudaSetDevice(s->device));
   StepParams p = make_params(s, b0, b1, s->dx, s->dy, s->dz, s->dt);
@@ -844,9 +903,14 @@ extern "C" void dc_device_add_source(dc_device_data *data, size_t index, float s
   }
   const long long i = static_cast<long long>(index);
   const long long x = i % s->sx, y = (i / s->sx) % s->sy, z = i / (s->sx * s->sy);
+  int cur = -1, prev = -1;
+  if (!roles(s, &cur, &prev)) {
+    set_error("field pointers rearranged");
+    abi_die("dc_device_add_source");
+  }
   ++s->launches;
-  cudaError_t e = launch_add_value(s->stream, data->pc, data->qc,
-                                   z * s->plane + y * s->pitch + x, source);
+  cudaError_t e = launch_add_value(s->stream, s->pq[cur], z * s->plane + y * s->pitch + x,
+                                   source);
   if (e != cudaSuccess) {
     set_error(cudaGetErrorString(e));
     abi_die("dc_device_add_source");
@@ -881,30 +945,34 @@ void halo_copy(dc_device_data *data, float *host, const size_t start[3], const s
     set_error("null argument");
     abi_die(where);
   }
+  const long long lim[3] = {s->sx, s->sy, s->sz};
   for (int d = 0; d < 3; ++d)
-    if (end[d] < start[d] || end[d] > sizes[d]) {
-      set_error("box outside the array");
+    if (end[d] < start[d] || static_cast<long long>(end[d]) > lim[d] ||
+        static_cast<long long>(sizes[d]) != lim[d]) {
+      set_error("box outside the array or sizes differ");
       abi_die(where);
     }
-  const size_t w = end[0] - start[0], hgt = end[1] - start[1], dep = end[2] - start[2];
-  if (w == 0 || hgt == 0 || dep == 0) return;
-  cudaMemcpy3DParms p{};
-  cudaPitchedPtr devp = make_cudaPitchedPtr(dev, s->pitch * 4, s->sx, s->sy);
-  cudaPitchedPtr hostp = make_cudaPitchedPtr(host, w * 4, w, hgt);
-  cudaPos devpos = make_cudaPos(start[0] * 4, start[1], start[2]);
-  if (to_host) {
-    p.srcPtr = devp;
-    p.srcPos = devpos;
-    p.dstPtr = hostp;
-    p.kind = cudaMemcpyDeviceToHost;
-  } else {
-    p.srcPtr = hostp;
-    p.dstPtr = devp;
-    p.dstPos = devpos;
-    p.kind = cudaMemcpyHostToDevice;
+  int comp = 0;
+  const int b = component_of(s, dev, &comp);
+  if (b < 0) {
+    set_error("array does not belong to this simulation");
+    abi_die(where);
   }
-  p.extent = make_cudaExtent(w * 4, hgt, dep);
-  cudaError_t e = cudaMemcpy3DAsync(&p, s->stream);
+  const long long b0[3] = {static_cast<long long>(start[0]), static_cast<long long>(start[1]),
+                           static_cast<long long>(start[2])};
+  const long long b1[3] = {static_cast<long long>(end[0]), static_cast<long long>(end[1]),
+                           static_cast<long long>(end[2])};
+  const long long n = (b1[0] - b0[0]) * (b1[1] - b0[1]) * (b1[2] - b0[2]);
+  if (n == 0) return;
+  float *stage = nullptr;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n, s->stream);
+  if (e == cudaSuccess && !to_host)
+    e = cudaMemcpyAsync(stage, host, sizeof(float) * n, cudaMemcpyHostToDevice, s->stream);
+  if (e == cudaSuccess)
+    e = launch_box_copy(s->stream, s->pq[b], comp, stage, b0, b1, s->pitch, s->plane, to_host);
+  if (e == cudaSuccess && to_host)
+    e = cudaMemcpyAsync(host, stage, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream);
+  if (stage) cudaFreeAsync(stage, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) {
     set_error(cudaGetErrorString(e));

@@ -77,17 +77,19 @@ struct H12 {
   float h1, h2;
 };
 
+// `f` points at one component of a pair buffer: element strides are doubled
+// (sX = 2, sY = 2*pitch, sZ = 2*plane, i = 2*index).
 __device__ __forceinline__ H12 hterms(const float *__restrict__ f, long long i,
-                                      long long sY, long long sZ,
+                                      long long sX, long long sY, long long sZ,
                                       const StepParams &prm, float cxx,
                                       float cyy, float czz, float cxy,
                                       float cyz, float cxz) {
-  const float fxx = der2_x(f, i, 1, prm.dxxinv);
+  const float fxx = der2_x(f, i, sX, prm.dxxinv);
   const float fyy = der2_x(f, i, sY, prm.dyyinv);
   const float fzz = der2_x(f, i, sZ, prm.dzzinv);
-  const float fxy = cross_x(f, i, 1, sY, prm.dxyinv);
+  const float fxy = cross_x(f, i, sX, sY, prm.dxyinv);
   const float fyz = cross_x(f, i, sY, sZ, prm.dyzinv);
-  const float fxz = cross_x(f, i, 1, sZ, prm.dxzinv);
+  const float fxz = cross_x(f, i, sX, sZ, prm.dxzinv);
   float h1 = __fmul_rn(cxx, fxx);
   h1 = __fadd_rn(h1, __fmul_rn(cyy, fyy));
   h1 = __fadd_rn(h1, __fmul_rn(czz, fzz));
@@ -139,8 +141,9 @@ __global__ void __launch_bounds__(128)
       v2px = __fmul_rn(v2pz, 1.48f);
       v2pn = __fmul_rn(v2pz, 1.2f);
     }
-    const H12 hp = hterms(prm.pc_in, i, sY, sZ, prm, cxx, cyy, czz, cxy, cyz, cxz);
-    const H12 hq = hterms(prm.qc_in, i, sY, sZ, prm, cxx, cyy, czz, cxy, cyz, cxz);
+    const float *pcf = reinterpret_cast<const float *>(prm.cur);
+    const H12 hp = hterms(pcf, 2 * i, 2, 2 * sY, 2 * sZ, prm, cxx, cyy, czz, cxy, cyz, cxz);
+    const H12 hq = hterms(pcf + 1, 2 * i, 2, 2 * sY, 2 * sZ, prm, cxx, cyy, czz, cxy, cyz, cxz);
     const float h1pmq = __fsub_rn(hp.h1, hq.h1);
     const float h2pmq = __fsub_rn(hp.h2, hq.h2);
     const float rhsp = __fadd_rn(
@@ -149,8 +152,10 @@ __global__ void __launch_bounds__(128)
     const float rhsq = __fsub_rn(
         __fadd_rn(__fmul_rn(v2pn, hp.h2), __fmul_rn(v2pz, hq.h1)),
         __fmul_rn(v2sz, h2pmq));
-    const float pc = __ldg(prm.pc_in + i), qc = __ldg(prm.qc_in + i);
-    const float ppo = prm.pp_out[i], qpo = prm.qp_out[i];
+    const float2 cv = prm.cur[i];
+    const float pc = cv.x, qc = cv.y;
+    const float2 pv = prm.prev[i];
+    const float ppo = pv.x, qpo = pv.y;
     const float tp = __fmul_rn(__fmul_rn(rhsp, prm.dt), prm.dt);
     const float tq = __fmul_rn(__fmul_rn(rhsq, prm.dt), prm.dt);
     float np, nq;
@@ -176,8 +181,7 @@ __global__ void __launch_bounds__(128)
       np = __fadd_rn(np, sv);
       nq = __fadd_rn(nq, sv);
     }
-    prm.pp_out[i] = np;
-    prm.qp_out[i] = nq;
+    prm.prev[i] = make_float2(np, nq);
   }
   if (prm.energy) {
     double e = static_cast<double>(e_acc);

@@ -44,47 +44,64 @@ struct FastLayout {
   static constexpr int NT = TX * TY;
   static constexpr int NCA = MEDIUM == DC_GB300_MEDIUM_PRECOMP ? 3 : 0;
   static constexpr int NCB = MEDIUM == DC_GB300_MEDIUM_PRECOMP ? 7 : 2;
-  static constexpr int HALO_BYTES = align128(HX * HY * 4);
-  static constexpr int TILE_BYTES = NT * 4;  // NT % 32 == 0: 128-B multiple
-  static constexpr int OFF_HP = 0;
-  static constexpr int OFF_HQ = HALO_BYTES;
-  static constexpr int OFF_CA = 2 * HALO_BYTES;
-  static constexpr int OFF_CB = OFF_CA + NCA * TILE_BYTES;
-  static constexpr int OFF_OWN = OFF_CB + NCB * TILE_BYTES;
-  static constexpr int STAGE_BYTES = OFF_OWN + 2 * TILE_BYTES;
-  static constexpr int DY_BYTES = align128(TY * HX * 4);
-  static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;  // [3 buffers][field]
-  static constexpr int OFF_BAR = OFF_DY + 3 * 2 * DY_BYTES;
+  // a halo plane of (p, q) pairs, HY rows of HX pairs
+  static constexpr int HALO_BYTES = align128(HX * HY * 8);
+  static constexpr int TILE4 = NT * 4;  // one coefficient tile (128-B multiple)
+  static constexpr int OFF_H = 0;
+  static constexpr int OFF_CA = HALO_BYTES;
+  static constexpr int OFF_CB = OFF_CA + NCA * TILE4;
+  static constexpr int OFF_OWN = OFF_CB + NCB * TILE4;  // (pp, qp) pairs
+  static constexpr int STAGE_BYTES = OFF_OWN + NT * 8;
+  static constexpr int DY_BYTES = align128(TY * HX * 8);  // (dy p, dy q) pairs
+  static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;     // 3 buffers
+  static constexpr int OFF_BAR = OFF_DY + 3 * DY_BYTES;
   static constexpr int SMEM_BYTES = OFF_BAR + NSTAGE * 8;
-  static constexpr uint32_t TX_HALO = 2u * HX * HY * 4u;
+  static constexpr uint32_t TX_HALO = HX * HY * 8u;
   static constexpr uint32_t TX_CA = NCA * NT * 4u;
-  static constexpr uint32_t TX_OUT = (NCB + 2) * NT * 4u;
+  static constexpr uint32_t TX_OUT = NCB * NT * 4u + NT * 8u;
   static_assert(TX % 32 == 0, "a warp spans one tile row");
-  static_assert(HX * 4 % 16 == 0, "TMA box rows are 16-byte multiples");
   static_assert(8 * TY <= NT, "halo-column work fits the CTA");
   static_assert(NSTAGE == 3, "stage index u % 3 is a compile-time constant");
 };
 
-// Second derivative with pre-scaled weights w[0..4] (K_i / da^2).
-__device__ __forceinline__ float d2w(const float *w, float c, float m1,
-                                     float p1, float m2, float p2, float m3,
-                                     float p3, float m4, float p4) {
-  float a = w[0] * c;
-  a = fmaf(w[1], m1 + p1, a);
-  a = fmaf(w[2], m2 + p2, a);
-  a = fmaf(w[3], m3 + p3, a);
-  a = fmaf(w[4], m4 + p4, a);
+// Packed FP32 pair arithmetic (one instruction updates p and q).
+__device__ __forceinline__ float2 bc(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  return __ffma2_rn(a, b, c);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+
+// Second derivative of a (p, q) pair with pre-scaled weights w[0..4]
+// (K_i / da^2).
+__device__ __forceinline__ float2 d2(const float *w, float2 c, float2 m1, float2 p1,
+                                     float2 m2, float2 p2, float2 m3, float2 p3,
+                                     float2 m4, float2 p4) {
+  float2 a = mul2(bc(w[0]), c);
+  a = fma2(bc(w[1]), m1, a);
+  a = fma2(bc(w[1]), p1, a);
+  a = fma2(bc(w[2]), m2, a);
+  a = fma2(bc(w[2]), p2, a);
+  a = fma2(bc(w[3]), m3, a);
+  a = fma2(bc(w[3]), p3, a);
+  a = fma2(bc(w[4]), m4, a);
+  a = fma2(bc(w[4]), p4, a);
   return a;
 }
 
-// First derivative with pre-scaled weights w[0..3] (L_i / da).
-__device__ __forceinline__ float d1w(const float *w, float m1, float p1,
-                                     float m2, float p2, float m3, float p3,
-                                     float m4, float p4) {
-  float a = w[0] * (p1 - m1);
-  a = fmaf(w[1], p2 - m2, a);
-  a = fmaf(w[2], p3 - m3, a);
-  a = fmaf(w[3], p4 - m4, a);
+// First derivative of a (p, q) pair with weights w (L_i / da) and their
+// negations n.
+__device__ __forceinline__ float2 d1(const float *w, const float *n, float2 m1, float2 p1,
+                                     float2 m2, float2 p2, float2 m3, float2 p3,
+                                     float2 m4, float2 p4) {
+  float2 a = mul2(bc(w[0]), p1);
+  a = fma2(bc(n[0]), m1, a);
+  a = fma2(bc(w[1]), p2, a);
+  a = fma2(bc(n[1]), m2, a);
+  a = fma2(bc(w[2]), p3, a);
+  a = fma2(bc(n[2]), m3, a);
+  a = fma2(bc(w[3]), p4, a);
+  a = fma2(bc(n[3]), m4, a);
   return a;
 }
 
@@ -97,10 +114,8 @@ constexpr float kV2pxFactor = 1.48f, kV2pnFactor = 1.2f;
 
 template <int TX, int TY, int MEDIUM, bool SPONGE>
 __global__ void __launch_bounds__(TX *TY, 1)
-    fast_kernel(const __grid_constant__ CUtensorMap tm_pc,
-                const __grid_constant__ CUtensorMap tm_qc,
-                const __grid_constant__ CUtensorMap tm_pp,
-                const __grid_constant__ CUtensorMap tm_qp,
+    fast_kernel(const __grid_constant__ CUtensorMap tm_cur,
+                const __grid_constant__ CUtensorMap tm_prev,
                 const __grid_constant__ CUtensorMap tm_ca,
                 const __grid_constant__ CUtensorMap tm_cb,
                 const __grid_constant__ StepParams prm) {
@@ -134,10 +149,8 @@ __global__ void __launch_bounds__(TX *TY, 1)
   if (tid == 0) {
     for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
     mbar_init_fence();
-    prefetch_tensormap(&tm_pc);
-    prefetch_tensormap(&tm_qc);
-    prefetch_tensormap(&tm_pp);
-    prefetch_tensormap(&tm_qp);
+    prefetch_tensormap(&tm_cur);
+    prefetch_tensormap(&tm_prev);
     prefetch_tensormap(&tm_cb);
     if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) prefetch_tensormap(&tm_ca);
   }
@@ -153,25 +166,23 @@ __global__ void __launch_bounds__(TX *TY, 1)
     const uint32_t bytes = Lay::TX_HALO + (want_ca ? Lay::TX_CA : 0u) +
                            (want_out ? Lay::TX_OUT : 0u);
     mbar_arrive_expect_tx(&bars[s], bytes);
-    tma_load_3d(st + Lay::OFF_HP, &tm_pc, x0 - kHalo, y0 - kHalo, k, &bars[s]);
-    tma_load_3d(st + Lay::OFF_HQ, &tm_qc, x0 - kHalo, y0 - kHalo, k, &bars[s]);
+    tma_load_3d(st + Lay::OFF_H, &tm_cur, x0 - kHalo, y0 - kHalo, k, &bars[s]);
     if (want_ca) tma_load_4d(st + Lay::OFF_CA, &tm_ca, x0, y0, k, 0, &bars[s]);
     if (want_out) {
       tma_load_4d(st + Lay::OFF_CB, &tm_cb, x0, y0, k - kHalo,
                   MEDIUM == DC_GB300_MEDIUM_PRECOMP ? 3 : 0, &bars[s]);
-      tma_load_3d(st + Lay::OFF_OWN, &tm_pp, x0, y0, k - kHalo, &bars[s]);
-      tma_load_3d(st + Lay::OFF_OWN + Lay::TILE_BYTES, &tm_qp, x0, y0,
-                  k - kHalo, &bars[s]);
+      tma_load_3d(st + Lay::OFF_OWN, &tm_prev, x0, y0, k - kHalo, &bars[s]);
     }
   };
 
   if (tid == 0)
     for (int j = 0; j < NSTAGE - 1 && j < n_it; ++j) issue(j);
 
-  // Register queues indexed by plane mod 9 (compile-time after unrolling).
-  float cqp[9], cqq[9], dxp[9], dxq[9], dyp[9], dyq[9];
-  float ap[9], bp[9], aq[9], bq[9];
-  float e_acc = 0.f;
+  // Register queues of (p, q) pairs indexed by plane mod 9 (compile-time
+  // after unrolling): centre value, x- and y-derivative, and the delayed
+  // in-plane parts A (of H1) and B (of the Laplacian).
+  float2 cq[9], dxq[9], dyq[9], aq[9], bq[9];
+  float2 e_acc = make_float2(0.f, 0.f);
   int abort_it = -1;
 
   // inactive threads of edge tiles may sit past the array: no profile read
@@ -184,10 +195,8 @@ __global__ void __launch_bounds__(TX *TY, 1)
   const int ot = ty * TX + tx;                    // centre in a tile
   // global position of this column at the first output plane (advanced by
   // one plane per output; never dereferenced for inactive threads)
-  const long long g0 = static_cast<long long>(zb) * prm.plane +
-                       static_cast<long long>(gy) * prm.pitch + gx;
-  float *out_p = prm.pp_out + g0;
-  float *out_q = prm.qp_out + g0;
+  float2 *out = prm.prev + (static_cast<long long>(zb) * prm.plane +
+                            static_cast<long long>(gy) * prm.pitch + gx);
 
   uint32_t mpar = 0;  // parity of the outer (9-plane) iteration
   for (int it0 = 0; it0 < n_it; it0 += 9, mpar ^= 1u) {
@@ -197,61 +206,38 @@ __global__ void __launch_bounds__(TX *TY, 1)
       if (it < n_it) {  // CTA-uniform
         // stage u % 3; its use count is it / 3 = 3 * (it0 / 9) + u / 3
         unsigned char *st = smem + (u % 3) * Lay::STAGE_BYTES;
-        uint64_t *bar = &bars[u % 3];
-        const bool ok =
-            mbar_wait_bounded(bar, mpar ^ static_cast<uint32_t>((u / 3) & 1), kWaitLimitNs);
-        const float *hp = reinterpret_cast<const float *>(st + Lay::OFF_HP);
-        const float *hq = reinterpret_cast<const float *>(st + Lay::OFF_HQ);
-        float *dybp = reinterpret_cast<float *>(smem + Lay::OFF_DY + (u % 3) * 2 * Lay::DY_BYTES);
-        float *dybq = dybp + Lay::DY_BYTES / 4;
+        const bool ok = mbar_wait_bounded(&bars[u % 3],
+                                          mpar ^ static_cast<uint32_t>((u / 3) & 1),
+                                          kWaitLimitNs);
+        const float2 *h = reinterpret_cast<const float2 *>(st + Lay::OFF_H);
+        float2 *dyb = reinterpret_cast<float2 *>(smem + Lay::OFF_DY + (u % 3) * Lay::DY_BYTES);
 
         // ---- leading plane k: centre, x/y second and first derivatives
-        float pxx, pyy, qxx, qyy;
+        float2 xx, yy;
         {
-          const float *h = hp;
-          const float c = h[c0];
-          const float xm1 = h[c0 - 1], xp1 = h[c0 + 1], xm2 = h[c0 - 2],
-                      xp2 = h[c0 + 2], xm3 = h[c0 - 3], xp3 = h[c0 + 3],
-                      xm4 = h[c0 - 4], xp4 = h[c0 + 4];
-          const float ym1 = h[c0 - HX], yp1 = h[c0 + HX],
-                      ym2 = h[c0 - 2 * HX], yp2 = h[c0 + 2 * HX],
-                      ym3 = h[c0 - 3 * HX], yp3 = h[c0 + 3 * HX],
-                      ym4 = h[c0 - 4 * HX], yp4 = h[c0 + 4 * HX];
-          pxx = d2w(prm.w2x, c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
-          pyy = d2w(prm.w2y, c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
-          cqp[u] = c;
-          dxp[u] = d1w(prm.w1x, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
-          dyp[u] = d1w(prm.w1y, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
-          dybp[od] = dyp[u];
-        }
-        {
-          const float *h = hq;
-          const float c = h[c0];
-          const float xm1 = h[c0 - 1], xp1 = h[c0 + 1], xm2 = h[c0 - 2],
-                      xp2 = h[c0 + 2], xm3 = h[c0 - 3], xp3 = h[c0 + 3],
-                      xm4 = h[c0 - 4], xp4 = h[c0 + 4];
-          const float ym1 = h[c0 - HX], yp1 = h[c0 + HX],
-                      ym2 = h[c0 - 2 * HX], yp2 = h[c0 + 2 * HX],
-                      ym3 = h[c0 - 3 * HX], yp3 = h[c0 + 3 * HX],
-                      ym4 = h[c0 - 4 * HX], yp4 = h[c0 + 4 * HX];
-          qxx = d2w(prm.w2x, c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
-          qyy = d2w(prm.w2y, c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
-          cqq[u] = c;
-          dxq[u] = d1w(prm.w1x, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
-          dyq[u] = d1w(prm.w1y, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
-          dybq[od] = dyq[u];
+          const float2 c = h[c0];
+          const float2 xm1 = h[c0 - 1], xp1 = h[c0 + 1], xm2 = h[c0 - 2],
+                       xp2 = h[c0 + 2], xm3 = h[c0 - 3], xp3 = h[c0 + 3],
+                       xm4 = h[c0 - 4], xp4 = h[c0 + 4];
+          const float2 ym1 = h[c0 - HX], yp1 = h[c0 + HX],
+                       ym2 = h[c0 - 2 * HX], yp2 = h[c0 + 2 * HX],
+                       ym3 = h[c0 - 3 * HX], yp3 = h[c0 + 3 * HX],
+                       ym4 = h[c0 - 4 * HX], yp4 = h[c0 + 4 * HX];
+          xx = d2(prm.w2x, c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
+          yy = d2(prm.w2y, c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
+          cq[u] = c;
+          dxq[u] = d1(prm.w1x, prm.n1x, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
+          dyq[u] = d1(prm.w1y, prm.n1y, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
+          dyb[od] = dyq[u];
         }
         // y-derivatives of the 4 + 4 halo columns (needed by d2/dxdy)
         if (tid < 8 * TY) {
           const int hc = tid & 7, hy = tid >> 3;
           const int hx = hc < 4 ? hc : TX + hc;
           const int o = (hy + kHalo) * HX + hx;
-          dybp[hy * HX + hx] =
-              d1w(prm.w1y, hp[o - HX], hp[o + HX], hp[o - 2 * HX], hp[o + 2 * HX],
-                  hp[o - 3 * HX], hp[o + 3 * HX], hp[o - 4 * HX], hp[o + 4 * HX]);
-          dybq[hy * HX + hx] =
-              d1w(prm.w1y, hq[o - HX], hq[o + HX], hq[o - 2 * HX], hq[o + 2 * HX],
-                  hq[o - 3 * HX], hq[o + 3 * HX], hq[o - 4 * HX], hq[o + 4 * HX]);
+          dyb[hy * HX + hx] =
+              d1(prm.w1y, prm.n1y, h[o - HX], h[o + HX], h[o - 2 * HX], h[o + 2 * HX],
+                 h[o - 3 * HX], h[o + 3 * HX], h[o - 4 * HX], h[o + 4 * HX]);
         }
         if (__syncthreads_or(!ok)) {
           abort_it = it;
@@ -260,14 +246,11 @@ __global__ void __launch_bounds__(TX *TY, 1)
         // The stage read in iteration it-1 is free: refill it.
         if (tid == 0 && it + NSTAGE - 1 < n_it) issue(it + NSTAGE - 1);
 
-        // ---- in-plane part of H1/H2 at plane k, delayed to output time
+        // ---- in-plane part of H1 and of the Laplacian at plane k
         if (it >= kHalo && it < n_it - kHalo) {
-          const float pxy = d1w(prm.w1x, dybp[od - 1], dybp[od + 1], dybp[od - 2],
-                                dybp[od + 2], dybp[od - 3], dybp[od + 3],
-                                dybp[od - 4], dybp[od + 4]);
-          const float qxy = d1w(prm.w1x, dybq[od - 1], dybq[od + 1], dybq[od - 2],
-                                dybq[od + 2], dybq[od - 3], dybq[od + 3],
-                                dybq[od - 4], dybq[od + 4]);
+          const float2 xy = d1(prm.w1x, prm.n1x, dyb[od - 1], dyb[od + 1], dyb[od - 2],
+                               dyb[od + 2], dyb[od - 3], dyb[od + 3], dyb[od - 4],
+                               dyb[od + 4]);
           float cxx, cyy, cxy;
           if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) {
             const float *ca = reinterpret_cast<const float *>(st + Lay::OFF_CA);
@@ -279,10 +262,8 @@ __global__ void __launch_bounds__(TX *TY, 1)
             cyy = kCyy;
             cxy = kCxy;
           }
-          ap[u] = fmaf(cxy, pxy, fmaf(cyy, pyy, cxx * pxx));
-          bp[u] = pxx + pyy;
-          aq[u] = fmaf(cxy, qxy, fmaf(cyy, qyy, cxx * qxx));
-          bq[u] = qxx + qyy;
+          aq[u] = fma2(bc(cxy), xy, fma2(bc(cyy), yy, mul2(bc(cxx), xx)));
+          bq[u] = add2(xx, yy);
         }
 
         // ---- output plane z = k - 4
@@ -291,20 +272,14 @@ __global__ void __launch_bounds__(TX *TY, 1)
           const int m4 = (u + 1) % 9, m3 = (u + 2) % 9, m2 = (u + 3) % 9,
                     m1 = (u + 4) % 9, c = (u + 5) % 9, p1 = (u + 6) % 9,
                     p2 = (u + 7) % 9, p3 = (u + 8) % 9, p4 = u;
-          const float pzz = d2w(prm.w2z, cqp[c], cqp[m1], cqp[p1], cqp[m2], cqp[p2],
-                                cqp[m3], cqp[p3], cqp[m4], cqp[p4]);
-          const float qzz = d2w(prm.w2z, cqq[c], cqq[m1], cqq[p1], cqq[m2], cqq[p2],
-                                cqq[m3], cqq[p3], cqq[m4], cqq[p4]);
-          const float pxz = d1w(prm.w1z, dxp[m1], dxp[p1], dxp[m2], dxp[p2], dxp[m3],
-                                dxp[p3], dxp[m4], dxp[p4]);
-          const float qxz = d1w(prm.w1z, dxq[m1], dxq[p1], dxq[m2], dxq[p2], dxq[m3],
-                                dxq[p3], dxq[m4], dxq[p4]);
-          const float pyz = d1w(prm.w1z, dyp[m1], dyp[p1], dyp[m2], dyp[p2], dyp[m3],
-                                dyp[p3], dyp[m4], dyp[p4]);
-          const float qyz = d1w(prm.w1z, dyq[m1], dyq[p1], dyq[m2], dyq[p2], dyq[m3],
-                                dyq[p3], dyq[m4], dyq[p4]);
+          const float2 zz = d2(prm.w2z, cq[c], cq[m1], cq[p1], cq[m2], cq[p2], cq[m3],
+                               cq[p3], cq[m4], cq[p4]);
+          const float2 xz = d1(prm.w1z, prm.n1z, dxq[m1], dxq[p1], dxq[m2], dxq[p2],
+                               dxq[m3], dxq[p3], dxq[m4], dxq[p4]);
+          const float2 yz = d1(prm.w1z, prm.n1z, dyq[m1], dyq[p1], dyq[m2], dyq[p2],
+                               dyq[m3], dyq[p3], dyq[m4], dyq[p4]);
           const float *cb = reinterpret_cast<const float *>(st + Lay::OFF_CB);
-          const float *own = reinterpret_cast<const float *>(st + Lay::OFF_OWN);
+          const float2 *own = reinterpret_cast<const float2 *>(st + Lay::OFF_OWN);
           float czz, cxz, cyz, v2px, v2pz, v2sz, v2pn;
           if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) {
             czz = cb[0 * NT + ot];
@@ -324,39 +299,36 @@ __global__ void __launch_bounds__(TX *TY, 1)
             v2px = v2pz * kV2pxFactor;
             v2pn = v2pz * kV2pnFactor;
           }
-          const float h1p = fmaf(cyz, pyz, fmaf(cxz, pxz, fmaf(czz, pzz, ap[c])));
-          const float h2p = bp[c] + pzz - h1p;
-          const float h1q = fmaf(cyz, qyz, fmaf(cxz, qxz, fmaf(czz, qzz, aq[c])));
-          const float h2q = bq[c] + qzz - h1q;
-          const float rhsp = fmaf(v2sz, h1p - h1q, fmaf(v2pz, h1q, v2px * h2p));
-          const float rhsq = fmaf(-v2sz, h2p - h2q, fmaf(v2pz, h1q, v2pn * h2p));
-          const float ppo = own[ot], qpo = own[NT + ot];
-          float np, nq;
+          // (h1p, h1q) and (h2p, h2q)
+          const float2 h1 = fma2(bc(cyz), yz, fma2(bc(cxz), xz, fma2(bc(czz), zz, aq[c])));
+          const float2 h2 = fma2(bc(-1.0f), h1, add2(bq[c], zz));
+          const float rhsp = fmaf(v2sz, h1.x - h1.y, fmaf(v2pz, h1.y, v2px * h2.x));
+          const float rhsq = fmaf(-v2sz, h2.x - h2.y, fmaf(v2pz, h1.y, v2pn * h2.x));
+          const float2 rhs = make_float2(rhsp, rhsq);
+          const float2 pv = own[ot];
+          const float2 cc = add2(cq[c], cq[c]);  // 2 * current
+          float2 nv;
           if (SPONGE) {
             const int z = zb + it - 2 * kHalo;
             const float g = gxy * prm.sponge[prm.sponge_oz + z];
-            np = fmaf(rhsp, prm.dt2, fmaf(-g, ppo, 2.0f * cqp[c])) * g;
-            nq = fmaf(rhsq, prm.dt2, fmaf(-g, qpo, 2.0f * cqq[c])) * g;
+            nv = mul2(fma2(rhs, bc(prm.dt2), fma2(bc(-g), pv, cc)), bc(g));
           } else {
-            np = fmaf(rhsp, prm.dt2, 2.0f * cqp[c] - ppo);
-            nq = fmaf(rhsq, prm.dt2, 2.0f * cqq[c] - qpo);
+            nv = fma2(rhs, bc(prm.dt2), fma2(bc(-1.0f), pv, cc));
           }
           if (active) {
-            if (prm.energy) e_acc = fmaf(np, np, fmaf(nq, nq, e_acc));
+            if (prm.energy) e_acc = fma2(nv, nv, e_acc);
             if (src_col && zb + it - 2 * kHalo == prm.src_z) {
               const int step = *prm.d_step + prm.step_offset;
               const float sv =
                   step + 1 < prm.src_count ? prm.src_table[step + 1] : 0.0f;
-              prm.src_pre[0] = np;
-              prm.src_pre[1] = nq;
-              np += sv;
-              nq += sv;
+              prm.src_pre[0] = nv.x;
+              prm.src_pre[1] = nv.y;
+              nv.x += sv;
+              nv.y += sv;
             }
-            *out_p = np;
-            *out_q = nq;
+            *out = nv;
           }
-          out_p += prm.plane;
-          out_q += prm.plane;
+          out += prm.plane;
         }
       }
     }
@@ -376,7 +348,7 @@ done:
   }
   if (prm.energy) {
     // CTA reduction of the float partials in double, one atomic per CTA.
-    double e = static_cast<double>(e_acc);
+    double e = static_cast<double>(e_acc.x) + static_cast<double>(e_acc.y);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) e += __shfl_down_sync(0xffffffffu, e, off);
     double *red = reinterpret_cast<double *>(smem + Lay::OFF_DY);
@@ -394,21 +366,18 @@ done:
 
 // Compiled tile shape.  TX = 32 (one warp per tile row), TY = 16 rows,
 // a 3-stage TMA ring.
-constexpr int kTX = 32, kTY = 16, kStages = 3;
+constexpr int kTX = 32, kTY = 12, kStages = 3;
 
 template <int MEDIUM, bool SPONGE>
-cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int pc_buf,
-                          int qc_buf, int pp_buf, int qp_buf) {
+cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int cur_buf, int prev_buf) {
   using Lay = FastLayout<kTX, kTY, kStages, MEDIUM>;
   auto kern = fast_kernel<kTX, kTY, MEDIUM, SPONGE>;
   const int nx = prm.x1 - prm.tile_x0, ny = prm.y1 - prm.tile_y0;
   const int nz = prm.z1 - prm.z0;
   dim3 grid((nx + kTX - 1) / kTX, (ny + kTY - 1) / kTY,
             (nz + prm.zchunk - 1) / prm.zchunk);
-  const CUtensorMap &cb = sim->tm_cb;
   kern<<<grid, kTX * kTY, Lay::SMEM_BYTES, sim->stream>>>(
-      sim->tm_halo[pc_buf], sim->tm_halo[qc_buf], sim->tm_own[pp_buf],
-      sim->tm_own[qp_buf], sim->tm_ca, cb, prm);
+      sim->tm_halo[cur_buf], sim->tm_own[prev_buf], sim->tm_ca, sim->tm_cb, prm);
   return cudaGetLastError();
 }
 
@@ -450,16 +419,20 @@ bool fast_encode_maps(Sim *sim, std::string *err) {
   const uint64_t dims3[3] = {static_cast<uint64_t>(sim->sx),
                              static_cast<uint64_t>(sim->sy),
                              static_cast<uint64_t>(sim->sz)};
-  const uint64_t str3[2] = {static_cast<uint64_t>(sim->pitch) * 4,
-                            static_cast<uint64_t>(sim->plane) * 4};
+  // (p, q) pair buffers: 8-byte elements
+  const uint64_t str_pq[2] = {static_cast<uint64_t>(sim->pitch) * 8,
+                              static_cast<uint64_t>(sim->plane) * 8};
   const uint32_t box_halo[3] = {kTX + 8, kTY + 8, 1};
   const uint32_t box_own[3] = {kTX, kTY, 1};
-  for (int b = 0; b < 4; ++b) {
-    if (!encode_tiled(&sim->tm_halo[b], sim->field[b], 3, dims3, str3, box_halo, err))
+  for (int b = 0; b < 2; ++b) {
+    if (!encode_tiled(&sim->tm_halo[b], sim->pq[b], 3, dims3, str_pq, box_halo, err, true))
       return false;
-    if (!encode_tiled(&sim->tm_own[b], sim->field[b], 3, dims3, str3, box_own, err))
+    if (!encode_tiled(&sim->tm_own[b], sim->pq[b], 3, dims3, str_pq, box_own, err, true))
       return false;
   }
+  // coefficient arrays: 4-byte elements
+  const uint64_t str3[2] = {static_cast<uint64_t>(sim->pitch) * 4,
+                            static_cast<uint64_t>(sim->plane) * 4};
   const uint64_t str4[3] = {str3[0], str3[1],
                             static_cast<uint64_t>(sim->count) * 4};
   if (sim->medium == DC_GB300_MEDIUM_PRECOMP) {
@@ -479,14 +452,13 @@ bool fast_encode_maps(Sim *sim, std::string *err) {
   return true;
 }
 
-cudaError_t launch_fast(Sim *sim, const StepParams &prm, int pc_buf,
-                        int qc_buf, int pp_buf, int qp_buf) {
+cudaError_t launch_fast(Sim *sim, const StepParams &prm, int cur_buf, int prev_buf) {
   const bool sp = prm.sponge != nullptr;
   if (sim->medium == DC_GB300_MEDIUM_PRECOMP)
-    return sp ? launch_fast_t<DC_GB300_MEDIUM_PRECOMP, true>(sim, prm, pc_buf, qc_buf, pp_buf, qp_buf)
-              : launch_fast_t<DC_GB300_MEDIUM_PRECOMP, false>(sim, prm, pc_buf, qc_buf, pp_buf, qp_buf);
-  return sp ? launch_fast_t<DC_GB300_MEDIUM_VPZ_VSV, true>(sim, prm, pc_buf, qc_buf, pp_buf, qp_buf)
-            : launch_fast_t<DC_GB300_MEDIUM_VPZ_VSV, false>(sim, prm, pc_buf, qc_buf, pp_buf, qp_buf);
+    return sp ? launch_fast_t<DC_GB300_MEDIUM_PRECOMP, true>(sim, prm, cur_buf, prev_buf)
+              : launch_fast_t<DC_GB300_MEDIUM_PRECOMP, false>(sim, prm, cur_buf, prev_buf);
+  return sp ? launch_fast_t<DC_GB300_MEDIUM_VPZ_VSV, true>(sim, prm, cur_buf, prev_buf)
+            : launch_fast_t<DC_GB300_MEDIUM_VPZ_VSV, false>(sim, prm, cur_buf, prev_buf);
 }
 
 }  // namespace dcg

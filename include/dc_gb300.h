@@ -75,9 +75,15 @@ typedef struct {
 } dc_process_t;
 
 /* include/device_data.h:11-15.  The field and medium pointers are device
- * pointers into this library's arrays.  Rows of a device array are `pitch`
- * floats apart, where pitch = sx rounded up to a multiple of 4 (pitch == sx
- * whenever sx % 4 == 0); dc_gb300_device_pitch() returns it. */
+ * pointers into this library's arrays, in this library's device layout:
+ *   - p and q are stored interleaved as (p, q) pairs, so qp == pp + 1 and
+ *     qc == pc + 1 and consecutive points of one field are 2 floats apart;
+ *   - rows are `pitch` points apart, pitch = sx rounded up to a multiple of
+ *     4 (dc_gb300_device_pitch());
+ *   - vpz/vsv and the ten precomp arrays are plain pitched float arrays.
+ * The reference's host code only hands these pointers back to the entry
+ * points below (src/worker.c:482-485, :500-501), which understand the
+ * layout; dc_device_data_get_results returns dense host arrays. */
 typedef struct {
   float *pp, *pc, *qp, *qc;
   float *vpz, *vsv;
