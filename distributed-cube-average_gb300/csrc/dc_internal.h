@@ -53,7 +53,6 @@ struct StepParams {
   // fast kernel: FD weights pre-scaled by the grid spacing
   float w2x[5], w2y[5], w2z[5];  // K_i / da^2 (second derivative)
   float w1x[4], w1y[4], w1z[4];  // L_i / da   (first derivative, i = 1..4)
-  float n1x[4], n1y[4], n1z[4];  // -L_i / da
   float dt, dt2;
   // Wavefields are stored as interleaved (p, q) pairs: `prev` holds
   // (pp, qp) and is updated in place, `cur` holds (pc, qc).

@@ -166,9 +166,6 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
       p.w1x[k] = static_cast<float>(L[k] / hx);
       p.w1y[k] = static_cast<float>(L[k] / hy);
       p.w1z[k] = static_cast<float>(L[k] / hz);
-      p.n1x[k] = -p.w1x[k];
-      p.n1y[k] = -p.w1y[k];
-      p.n1z[k] = -p.w1z[k];
     }
   }
   p.dt = dt;

@@ -26,6 +26,7 @@
 // qp and ten coefficients, write pp and qp: 64 bytes (32 bytes for the
 // vpz/vsv medium form).
 #include <cstdio>
+#include <cstdlib>
 
 #include "dc_internal.h"
 #include "dc_ptx.cuh"
@@ -54,7 +55,10 @@ struct FastLayout {
   static constexpr int STAGE_BYTES = OFF_OWN + NT * 8;
   static constexpr int DY_BYTES = align128(TY * HX * 8);  // (dy p, dy q) pairs
   static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;     // 3 buffers
-  static constexpr int OFF_BAR = OFF_DY + 3 * DY_BYTES;
+  // per-thread ring of the delayed in-plane terms (A_p, A_q, B_p, B_q) of
+  // the last 9 planes
+  static constexpr int OFF_AB = OFF_DY + 3 * DY_BYTES;
+  static constexpr int OFF_BAR = OFF_AB + 9 * NT * 16;
   static constexpr int SMEM_BYTES = OFF_BAR + NSTAGE * 8;
   static constexpr uint32_t TX_HALO = HX * HY * 8u;
   static constexpr uint32_t TX_CA = NCA * NT * 4u;
@@ -73,36 +77,27 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 
 // Second derivative of a (p, q) pair with pre-scaled weights w[0..4]
-// (K_i / da^2).
+// (K_i / da^2), summed as two independent chains for instruction-level
+// parallelism.
 __device__ __forceinline__ float2 d2(const float *w, float2 c, float2 m1, float2 p1,
                                      float2 m2, float2 p2, float2 m3, float2 p3,
                                      float2 m4, float2 p4) {
-  float2 a = mul2(bc(w[0]), c);
-  a = fma2(bc(w[1]), m1, a);
-  a = fma2(bc(w[1]), p1, a);
-  a = fma2(bc(w[2]), m2, a);
-  a = fma2(bc(w[2]), p2, a);
-  a = fma2(bc(w[3]), m3, a);
-  a = fma2(bc(w[3]), p3, a);
-  a = fma2(bc(w[4]), m4, a);
-  a = fma2(bc(w[4]), p4, a);
-  return a;
+  const float2 s1 = add2(m1, p1), s2 = add2(m2, p2), s3 = add2(m3, p3), s4 = add2(m4, p4);
+  float2 t0 = fma2(bc(w[1]), s1, mul2(bc(w[0]), c));
+  const float2 t1 = fma2(bc(w[3]), s3, mul2(bc(w[2]), s2));
+  t0 = fma2(bc(w[4]), s4, t0);
+  return add2(t0, t1);
 }
 
-// First derivative of a (p, q) pair with weights w (L_i / da) and their
-// negations n.
-__device__ __forceinline__ float2 d1(const float *w, const float *n, float2 m1, float2 p1,
-                                     float2 m2, float2 p2, float2 m3, float2 p3,
-                                     float2 m4, float2 p4) {
-  float2 a = mul2(bc(w[0]), p1);
-  a = fma2(bc(n[0]), m1, a);
-  a = fma2(bc(w[1]), p2, a);
-  a = fma2(bc(n[1]), m2, a);
-  a = fma2(bc(w[2]), p3, a);
-  a = fma2(bc(n[2]), m3, a);
-  a = fma2(bc(w[3]), p4, a);
-  a = fma2(bc(n[3]), m4, a);
-  return a;
+// First derivative of a (p, q) pair with weights w[0..3] (L_i / da).
+__device__ __forceinline__ float2 d1(const float *w, float2 m1, float2 p1, float2 m2,
+                                     float2 p2, float2 m3, float2 p3, float2 m4, float2 p4) {
+  const float2 n = bc(-1.0f);
+  const float2 e1 = fma2(n, m1, p1), e2 = fma2(n, m2, p2), e3 = fma2(n, m3, p3),
+               e4 = fma2(n, m4, p4);
+  const float2 t0 = fma2(bc(w[2]), e3, mul2(bc(w[0]), e1));
+  const float2 t1 = fma2(bc(w[3]), e4, mul2(bc(w[1]), e2));
+  return add2(t0, t1);
 }
 
 // Constant-angle factors of the reference CUDA backend
@@ -112,8 +107,8 @@ constexpr float kCxy = 0.4546487134f, kCyz = 0.8414709848f;
 constexpr float kCxz = 0.5403023059f;
 constexpr float kV2pxFactor = 1.48f, kV2pnFactor = 1.2f;
 
-template <int TX, int TY, int MEDIUM, bool SPONGE>
-__global__ void __launch_bounds__(TX *TY, 1)
+template <int TX, int TY, int MEDIUM, bool SPONGE, bool ISO>
+__global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     fast_kernel(const __grid_constant__ CUtensorMap tm_cur,
                 const __grid_constant__ CUtensorMap tm_prev,
                 const __grid_constant__ CUtensorMap tm_ca,
@@ -123,6 +118,10 @@ __global__ void __launch_bounds__(TX *TY, 1)
   using Lay = FastLayout<TX, TY, NSTAGE, MEDIUM>;
   constexpr int HX = Lay::HX;
   constexpr int NT = Lay::NT;
+  // equal spacing on all axes: one set of weights serves x, y and z
+  const float *w2x = prm.w2x, *w1x = prm.w1x;
+  const float *w2y = ISO ? prm.w2x : prm.w2y, *w1y = ISO ? prm.w1x : prm.w1y;
+  const float *w2z = ISO ? prm.w2x : prm.w2z, *w1z = ISO ? prm.w1x : prm.w1z;
   // No static shared memory in this kernel: the dynamic window starts at
   // the CTA's shared base, so this alignment holds and every access below
   // is a shared-space access at a compile-time offset.
@@ -181,7 +180,8 @@ __global__ void __launch_bounds__(TX *TY, 1)
   // Register queues of (p, q) pairs indexed by plane mod 9 (compile-time
   // after unrolling): centre value, x- and y-derivative, and the delayed
   // in-plane parts A (of H1) and B (of the Laplacian).
-  float2 cq[9], dxq[9], dyq[9], aq[9], bq[9];
+  float2 cq[9], dxq[9], dyq[9];
+  float4 *abr = reinterpret_cast<float4 *>(smem + Lay::OFF_AB);
   float2 e_acc = make_float2(0.f, 0.f);
   int abort_it = -1;
 
@@ -223,11 +223,11 @@ __global__ void __launch_bounds__(TX *TY, 1)
                        ym2 = h[c0 - 2 * HX], yp2 = h[c0 + 2 * HX],
                        ym3 = h[c0 - 3 * HX], yp3 = h[c0 + 3 * HX],
                        ym4 = h[c0 - 4 * HX], yp4 = h[c0 + 4 * HX];
-          xx = d2(prm.w2x, c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
-          yy = d2(prm.w2y, c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
+          xx = d2(w2x, c, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
+          yy = d2(w2y, c, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
           cq[u] = c;
-          dxq[u] = d1(prm.w1x, prm.n1x, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
-          dyq[u] = d1(prm.w1y, prm.n1y, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
+          dxq[u] = d1(w1x, xm1, xp1, xm2, xp2, xm3, xp3, xm4, xp4);
+          dyq[u] = d1(w1y, ym1, yp1, ym2, yp2, ym3, yp3, ym4, yp4);
           dyb[od] = dyq[u];
         }
         // y-derivatives of the 4 + 4 halo columns (needed by d2/dxdy)
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(TX *TY, 1)
           const int hx = hc < 4 ? hc : TX + hc;
           const int o = (hy + kHalo) * HX + hx;
           dyb[hy * HX + hx] =
-              d1(prm.w1y, prm.n1y, h[o - HX], h[o + HX], h[o - 2 * HX], h[o + 2 * HX],
+              d1(w1y, h[o - HX], h[o + HX], h[o - 2 * HX], h[o + 2 * HX],
                  h[o - 3 * HX], h[o + 3 * HX], h[o - 4 * HX], h[o + 4 * HX]);
         }
         if (__syncthreads_or(!ok)) {
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(TX *TY, 1)
 
         // ---- in-plane part of H1 and of the Laplacian at plane k
         if (it >= kHalo && it < n_it - kHalo) {
-          const float2 xy = d1(prm.w1x, prm.n1x, dyb[od - 1], dyb[od + 1], dyb[od - 2],
+          const float2 xy = d1(w1x, dyb[od - 1], dyb[od + 1], dyb[od - 2],
                                dyb[od + 2], dyb[od - 3], dyb[od + 3], dyb[od - 4],
                                dyb[od + 4]);
           float cxx, cyy, cxy;
@@ -262,8 +262,9 @@ __global__ void __launch_bounds__(TX *TY, 1)
             cyy = kCyy;
             cxy = kCxy;
           }
-          aq[u] = fma2(bc(cxy), xy, fma2(bc(cyy), yy, mul2(bc(cxx), xx)));
-          bq[u] = add2(xx, yy);
+          const float2 av = fma2(bc(cxy), xy, fma2(bc(cyy), yy, mul2(bc(cxx), xx)));
+          const float2 bv = add2(xx, yy);
+          abr[u * NT + ot] = make_float4(av.x, av.y, bv.x, bv.y);
         }
 
         // ---- output plane z = k - 4
@@ -272,11 +273,12 @@ __global__ void __launch_bounds__(TX *TY, 1)
           const int m4 = (u + 1) % 9, m3 = (u + 2) % 9, m2 = (u + 3) % 9,
                     m1 = (u + 4) % 9, c = (u + 5) % 9, p1 = (u + 6) % 9,
                     p2 = (u + 7) % 9, p3 = (u + 8) % 9, p4 = u;
-          const float2 zz = d2(prm.w2z, cq[c], cq[m1], cq[p1], cq[m2], cq[p2], cq[m3],
+          const float4 ab = abr[c * NT + ot];  // A, B of plane z (own column)
+          const float2 zz = d2(w2z, cq[c], cq[m1], cq[p1], cq[m2], cq[p2], cq[m3],
                                cq[p3], cq[m4], cq[p4]);
-          const float2 xz = d1(prm.w1z, prm.n1z, dxq[m1], dxq[p1], dxq[m2], dxq[p2],
+          const float2 xz = d1(w1z, dxq[m1], dxq[p1], dxq[m2], dxq[p2],
                                dxq[m3], dxq[p3], dxq[m4], dxq[p4]);
-          const float2 yz = d1(prm.w1z, prm.n1z, dyq[m1], dyq[p1], dyq[m2], dyq[p2],
+          const float2 yz = d1(w1z, dyq[m1], dyq[p1], dyq[m2], dyq[p2],
                                dyq[m3], dyq[p3], dyq[m4], dyq[p4]);
           const float *cb = reinterpret_cast<const float *>(st + Lay::OFF_CB);
           const float2 *own = reinterpret_cast<const float2 *>(st + Lay::OFF_OWN);
@@ -300,8 +302,9 @@ __global__ void __launch_bounds__(TX *TY, 1)
             v2pn = v2pz * kV2pnFactor;
           }
           // (h1p, h1q) and (h2p, h2q)
-          const float2 h1 = fma2(bc(cyz), yz, fma2(bc(cxz), xz, fma2(bc(czz), zz, aq[c])));
-          const float2 h2 = fma2(bc(-1.0f), h1, add2(bq[c], zz));
+          const float2 h1 = fma2(bc(cyz), yz,
+                                 fma2(bc(cxz), xz, fma2(bc(czz), zz, make_float2(ab.x, ab.y))));
+          const float2 h2 = fma2(bc(-1.0f), h1, add2(make_float2(ab.z, ab.w), zz));
           const float rhsp = fmaf(v2sz, h1.x - h1.y, fmaf(v2pz, h1.y, v2px * h2.x));
           const float rhsq = fmaf(-v2sz, h2.x - h2.y, fmaf(v2pz, h1.y, v2pn * h2.x));
           const float2 rhs = make_float2(rhsp, rhsq);
@@ -364,28 +367,56 @@ done:
   }
 }
 
-// Compiled tile shape.  TX = 32 (one warp per tile row), TY = 16 rows,
-// a 3-stage TMA ring.
-constexpr int kTX = 32, kTY = 12, kStages = 3;
+// Compiled tile shapes: TX = 32 (one warp per tile row) and TY = 12 or 16
+// rows (384 or 512 threads), a 3-stage TMA ring.
+constexpr int kTX = 32, kStages = 3;
 
-template <int MEDIUM, bool SPONGE>
+template <int TY, int MEDIUM, bool SPONGE, bool ISO>
 cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int cur_buf, int prev_buf) {
-  using Lay = FastLayout<kTX, kTY, kStages, MEDIUM>;
-  auto kern = fast_kernel<kTX, kTY, MEDIUM, SPONGE>;
+  using Lay = FastLayout<kTX, TY, kStages, MEDIUM>;
+  auto kern = fast_kernel<kTX, TY, MEDIUM, SPONGE, ISO>;
   const int nx = prm.x1 - prm.tile_x0, ny = prm.y1 - prm.tile_y0;
   const int nz = prm.z1 - prm.z0;
-  dim3 grid((nx + kTX - 1) / kTX, (ny + kTY - 1) / kTY,
-            (nz + prm.zchunk - 1) / prm.zchunk);
-  kern<<<grid, kTX * kTY, Lay::SMEM_BYTES, sim->stream>>>(
+  dim3 grid((nx + kTX - 1) / kTX, (ny + TY - 1) / TY, (nz + prm.zchunk - 1) / prm.zchunk);
+  kern<<<grid, kTX * TY, Lay::SMEM_BYTES, sim->stream>>>(
       sim->tm_halo[cur_buf], sim->tm_own[prev_buf], sim->tm_ca, sim->tm_cb, prm);
   return cudaGetLastError();
 }
 
-template <int MEDIUM, bool SPONGE>
-cudaError_t set_smem_attr() {
-  using Lay = FastLayout<kTX, kTY, kStages, MEDIUM>;
-  return cudaFuncSetAttribute(fast_kernel<kTX, kTY, MEDIUM, SPONGE>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM_BYTES);
+template <int TY, int MEDIUM>
+cudaError_t set_smem_attr_all() {
+  using Lay = FastLayout<kTX, TY, kStages, MEDIUM>;
+  cudaError_t e = cudaSuccess;
+  const int b = Lay::SMEM_BYTES;
+  const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, MEDIUM, false, false>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, MEDIUM, false, true>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, MEDIUM, true, false>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, MEDIUM, true, true>, attr, b);
+  return e;
+}
+
+template <int TY>
+cudaError_t launch_ty(Sim *sim, const StepParams &prm, int cur, int prev) {
+  const bool sp = prm.sponge != nullptr;
+  const bool iso = sim->dx == sim->dy && sim->dy == sim->dz;
+  constexpr int P = DC_GB300_MEDIUM_PRECOMP, V = DC_GB300_MEDIUM_VPZ_VSV;
+  if (sim->medium == P) {
+    if (sp) return iso ? launch_fast_t<TY, P, true, true>(sim, prm, cur, prev)
+                       : launch_fast_t<TY, P, true, false>(sim, prm, cur, prev);
+    return iso ? launch_fast_t<TY, P, false, true>(sim, prm, cur, prev)
+               : launch_fast_t<TY, P, false, false>(sim, prm, cur, prev);
+  }
+  if (sp) return iso ? launch_fast_t<TY, V, true, true>(sim, prm, cur, prev)
+                     : launch_fast_t<TY, V, true, false>(sim, prm, cur, prev);
+  return iso ? launch_fast_t<TY, V, false, true>(sim, prm, cur, prev)
+             : launch_fast_t<TY, V, false, false>(sim, prm, cur, prev);
+}
+
+int chosen_ty() {
+  const char *e = std::getenv("DC_GB300_FAST_TY");
+  const int v = e ? std::atoi(e) : 0;
+  return (v == 8 || v == 12) ? v : 16;
 }
 
 }  // namespace
@@ -393,25 +424,31 @@ cudaError_t set_smem_attr() {
 FastShape fast_shape(const Sim *sim) {
   // z-chunk: enough CTAs for several waves over 152 SMs while keeping the
   // 8-plane warm-up of each chunk small.
+  const int ty = sim->maps_ty ? sim->maps_ty : chosen_ty();
   const long long tiles = ((sim->sx - 8 + kTX - 1) / kTX + 1) *
-                          ((sim->sy - 8 + kTY - 1) / kTY);
+                          ((sim->sy - 8 + ty - 1) / ty);
   const long long nzc = sim->sz - 8;
   long long chunks = (4 * 152 + tiles - 1) / tiles;
   long long zc = (nzc + chunks - 1) / chunks;
   if (zc < 32) zc = 32;
   if (zc > nzc) zc = nzc;
-  return FastShape{kTX, kTY, static_cast<int>(zc)};
+  return FastShape{kTX, ty, static_cast<int>(zc)};
 }
 
 bool fast_encode_maps(Sim *sim, std::string *err) {
   // dynamic shared memory above 48 KB must be enabled per kernel and device
   // (done here, before any stream capture)
-  cudaError_t ae = sim->medium == DC_GB300_MEDIUM_PRECOMP
-                       ? set_smem_attr<DC_GB300_MEDIUM_PRECOMP, false>()
-                       : set_smem_attr<DC_GB300_MEDIUM_VPZ_VSV, false>();
-  if (ae == cudaSuccess)
-    ae = sim->medium == DC_GB300_MEDIUM_PRECOMP ? set_smem_attr<DC_GB300_MEDIUM_PRECOMP, true>()
-                                                : set_smem_attr<DC_GB300_MEDIUM_VPZ_VSV, true>();
+  const int kTY = chosen_ty();
+  cudaError_t ae;
+  if (kTY == 8)
+    ae = sim->medium == DC_GB300_MEDIUM_PRECOMP ? set_smem_attr_all<8, DC_GB300_MEDIUM_PRECOMP>()
+                                                : set_smem_attr_all<8, DC_GB300_MEDIUM_VPZ_VSV>();
+  else if (kTY == 12)
+    ae = sim->medium == DC_GB300_MEDIUM_PRECOMP ? set_smem_attr_all<12, DC_GB300_MEDIUM_PRECOMP>()
+                                                : set_smem_attr_all<12, DC_GB300_MEDIUM_VPZ_VSV>();
+  else
+    ae = sim->medium == DC_GB300_MEDIUM_PRECOMP ? set_smem_attr_all<16, DC_GB300_MEDIUM_PRECOMP>()
+                                                : set_smem_attr_all<16, DC_GB300_MEDIUM_VPZ_VSV>();
   if (ae != cudaSuccess) {
     *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(ae);
     return false;
@@ -453,12 +490,9 @@ bool fast_encode_maps(Sim *sim, std::string *err) {
 }
 
 cudaError_t launch_fast(Sim *sim, const StepParams &prm, int cur_buf, int prev_buf) {
-  const bool sp = prm.sponge != nullptr;
-  if (sim->medium == DC_GB300_MEDIUM_PRECOMP)
-    return sp ? launch_fast_t<DC_GB300_MEDIUM_PRECOMP, true>(sim, prm, cur_buf, prev_buf)
-              : launch_fast_t<DC_GB300_MEDIUM_PRECOMP, false>(sim, prm, cur_buf, prev_buf);
-  return sp ? launch_fast_t<DC_GB300_MEDIUM_VPZ_VSV, true>(sim, prm, cur_buf, prev_buf)
-            : launch_fast_t<DC_GB300_MEDIUM_VPZ_VSV, false>(sim, prm, cur_buf, prev_buf);
+  if (sim->maps_ty == 8) return launch_ty<8>(sim, prm, cur_buf, prev_buf);
+  if (sim->maps_ty == 12) return launch_ty<12>(sim, prm, cur_buf, prev_buf);
+  return launch_ty<16>(sim, prm, cur_buf, prev_buf);
 }
 
 }  // namespace dcg
