@@ -317,7 +317,8 @@ def run_ours(args, rank, world, local):
     stencil_ms = ms / args.steps  # graph-replayed region: one stencil launch per step
     achieved = BYTES_PER_UPDATE * pts / (stencil_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    traffic_pp = profiled_traffic("tti_fast_config2.md") if kernel == dc.KERNEL_FAST else None
+    traffic_pp = (profiled_traffic("tti_fast_config2.md")
+                  if kernel == dc.KERNEL_FAST and args.n == N_INTERIOR else None)
     out_fields = sim.get_fields() if not args.no_cpu_baseline else None
     sim.close()
 
