@@ -159,6 +159,8 @@ SIGNATURES = [
     ("dc_gb300_synchronize", C.c_int, [C.c_void_p]),
     ("dc_gb300_steps_done", C.c_long, [C.c_void_p]),
     ("dc_gb300_propagate_box", C.c_int, [C.c_void_p, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    ("dc_gb300_save_checkpoint", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("dc_gb300_load_checkpoint", C.c_int, [C.c_void_p, C.c_char_p]),
     ("dc_gb300_kernel_launches", C.c_long, [C.c_void_p]),
     ("dc_gb300_stream", C.c_void_p, [C.c_void_p]),
     ("dc_gb300_source", C.c_float, [C.c_float, C.c_int, C.c_double]),
@@ -473,6 +475,12 @@ class Simulation:
 
     def propagate_box(self, start, end) -> None:
         check(lib().dc_gb300_propagate_box(self.h, _sz3(*start), _sz3(*end)))
+
+    def save_checkpoint(self, path) -> None:
+        check(lib().dc_gb300_save_checkpoint(self.h, str(path).encode()))
+
+    def load_checkpoint(self, path) -> None:
+        check(lib().dc_gb300_load_checkpoint(self.h, str(path).encode()))
 
     @property
     def steps_done(self) -> int:

@@ -20,6 +20,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "build"
 LIB = PKG / "libdc_gb300.so"
+CLI_SRC = PKG / "cli" / "dc_gb300_main.c"
+CLI = PKG / "dc_gb300"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -79,6 +81,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(_compile, srcs))
     if LIB.exists() and all(o.stat().st_mtime <= LIB.stat().st_mtime for o in objs):
+        build_cli()
         return LIB
     tmp = LIB.with_suffix(f".so.tmp{os.getpid()}")
     cmd = [nvcc(), "-shared", "-o", str(tmp), *map(str, objs), *ARCH,
@@ -90,7 +93,24 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     stamp.write_text(platform.machine())
     if verbose:
         print(f"built {LIB}")
+    build_cli(force=True)
     return LIB
+
+
+def build_cli(force: bool = False) -> Path:
+    """The command-line driver (cli/dc_gb300_main.c), linked against the
+    library with an $ORIGIN run path."""
+    deps = [CLI_SRC, LIB, INCLUDE / "dc_gb300.h"]
+    if not force and CLI.exists() and all(d.stat().st_mtime <= CLI.stat().st_mtime for d in deps):
+        return CLI
+    tmp = CLI.with_name(f"{CLI.name}.tmp{os.getpid()}")
+    cmd = ["gcc", "-O2", "-std=gnu11", "-Wall", str(CLI_SRC), "-I", str(INCLUDE),
+           "-L", str(PKG), "-ldc_gb300", "-Wl,-rpath,$ORIGIN", "-lm", "-o", str(tmp)]
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{proc.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":

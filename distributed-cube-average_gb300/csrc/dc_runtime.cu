@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -574,6 +575,114 @@ extern "C" int dc_gb300_get_fields(dc_gb300_sim *h, float *pp, float *pc, float 
   }
   DCG_TRY(cudaFreeAsync(stage, s->stream));
   DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+namespace {
+constexpr char kCkptMagic[8] = {'D', 'C', 'G', 'B', '3', '0', '0', 'C'};
+struct CkptHeader {
+  char magic[8];
+  uint32_t version, reserved;
+  int64_t sx, sy, sz, steps_done, src_applied, pad;
+};
+static_assert(sizeof(CkptHeader) == 64, "checkpoint header is 64 bytes");
+}  // namespace
+
+extern "C" int dc_gb300_save_checkpoint(dc_gb300_sim *h, const char *path) {
+  Sim *s = impl(h);
+  if (!s || !path) return fail(DC_GB300_ERR_ARG, "null argument");
+  DCG_TRY(cudaSetDevice(s->device));
+  int cur = -1, prev = -1;
+  if (!roles(s, &cur, &prev)) return fail(DC_GB300_ERR_STATE, "field pointers rearranged");
+  const long long n = s->sx * s->sy * s->sz;
+  std::vector<float> host(static_cast<size_t>(n) * 2);
+  float *stage = nullptr;
+  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
+  FILE *f = std::fopen(path, "wb");
+  if (!f) {
+    cudaFreeAsync(stage, s->stream);
+    return fail(DC_GB300_ERR_ARG, std::string("cannot open ") + path);
+  }
+  CkptHeader hd{};
+  std::memcpy(hd.magic, kCkptMagic, 8);
+  hd.version = 1;
+  hd.sx = s->sx;
+  hd.sy = s->sy;
+  hd.sz = s->sz;
+  hd.steps_done = s->steps_done;
+  hd.src_applied = (s->src_gi >= 0 && s->src_applied_step == s->steps_done) ? 1 : 0;
+  bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1;
+  for (int b : {prev, cur}) {
+    if (!ok) break;
+    cudaError_t e = launch_unpack(s->stream, s->pq[b], stage, stage + n, s->sx, s->sy, s->sz,
+                                  s->pitch);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(host.data(), stage, sizeof(float) * n * 2, cudaMemcpyDeviceToHost,
+                          s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) {
+      std::fclose(f);
+      cudaFreeAsync(stage, s->stream);
+      return fail(DC_GB300_ERR_CUDA, cudaGetErrorString(e));
+    }
+    ok = std::fwrite(host.data(), sizeof(float), host.size(), f) == host.size();
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  DCG_TRY(cudaFreeAsync(stage, s->stream));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  if (!ok) return fail(DC_GB300_ERR_ARG, std::string("write failed: ") + path);
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_load_checkpoint(dc_gb300_sim *h, const char *path) {
+  Sim *s = impl(h);
+  if (!s || !path) return fail(DC_GB300_ERR_ARG, "null argument");
+  DCG_TRY(cudaSetDevice(s->device));
+  int cur = -1, prev = -1;
+  if (!roles(s, &cur, &prev)) return fail(DC_GB300_ERR_STATE, "field pointers rearranged");
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return fail(DC_GB300_ERR_ARG, std::string("cannot open ") + path);
+  CkptHeader hd{};
+  if (std::fread(&hd, sizeof(hd), 1, f) != 1 || std::memcmp(hd.magic, kCkptMagic, 8) != 0 ||
+      hd.version != 1) {
+    std::fclose(f);
+    return fail(DC_GB300_ERR_ARG, "not a dc_gb300 checkpoint");
+  }
+  if (hd.sx != s->sx || hd.sy != s->sy || hd.sz != s->sz || hd.steps_done < 0 ||
+      hd.steps_done > (1LL << 30)) {
+    std::fclose(f);
+    return fail(DC_GB300_ERR_ARG, "checkpoint sizes differ from the simulation's");
+  }
+  const long long n = s->sx * s->sy * s->sz;
+  std::vector<float> host(static_cast<size_t>(n) * 2);
+  float *stage = nullptr;
+  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
+  for (int b : {prev, cur}) {
+    if (std::fread(host.data(), sizeof(float), host.size(), f) != host.size()) {
+      std::fclose(f);
+      cudaFreeAsync(stage, s->stream);
+      return fail(DC_GB300_ERR_ARG, "truncated checkpoint");
+    }
+    cudaError_t e = cudaMemcpyAsync(stage, host.data(), sizeof(float) * n * 2,
+                                    cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+      e = cudaMemsetAsync(s->pq[b], 0, sizeof(float2) * s->count, s->stream);
+    if (e == cudaSuccess)
+      e = launch_pack(s->stream, s->pq[b], stage, stage + n, s->sx, s->sy, s->sz, s->pitch);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) {
+      std::fclose(f);
+      cudaFreeAsync(stage, s->stream);
+      return fail(DC_GB300_ERR_CUDA, cudaGetErrorString(e));
+    }
+  }
+  std::fclose(f);
+  DCG_TRY(cudaFreeAsync(stage, s->stream));
+  const int step = static_cast<int>(hd.steps_done);
+  DCG_TRY(cudaMemcpyAsync(s->d_step, &step, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  s->steps_done = hd.steps_done;
+  s->src_applied_step = hd.src_applied ? hd.steps_done : -1;
   return DC_GB300_OK;
 }
 

@@ -314,6 +314,14 @@ long dc_gb300_steps_done(const dc_gb300_sim *sim);
 int dc_gb300_propagate_box(dc_gb300_sim *sim, const size_t start[3],
                            const size_t end[3]);
 
+/* Checkpoint / resume.  The file holds a 64-byte header (magic "DCGB300C",
+ * version 1, sx, sy, sz, steps done, whether pc/qc already contain the next
+ * step's source) followed by the dense float32 arrays pp, qp, pc, qc.
+ * Loading requires a simulation of the same sizes and restores the step
+ * counter, so a resumed run continues bit-identically.  Synchronous. */
+int dc_gb300_save_checkpoint(dc_gb300_sim *sim, const char *path);
+int dc_gb300_load_checkpoint(dc_gb300_sim *sim, const char *path);
+
 /* Kernel launches issued by this simulation so far (stencil + helpers). */
 long dc_gb300_kernel_launches(const dc_gb300_sim *sim);
 
