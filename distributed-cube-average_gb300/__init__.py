@@ -147,6 +147,8 @@ SIGNATURES = [
     ("dc_gb300_get_precomp", C.c_int, [C.c_void_p, C.POINTER(PrecompVars)]),
     ("dc_gb300_get_vpz_vsv", C.c_int, [C.c_void_p, _fp, _fp]),
     ("dc_gb300_generate_layered", C.c_int, [C.c_void_p, C.POINTER(LayeredSpec)]),
+    ("dc_gb300_generate_reference", C.c_int, [C.c_void_p, C.c_long, C.c_long, C.c_long,
+                                              C.c_long, C.c_uint]),
     ("dc_gb300_set_fields", C.c_int, [C.c_void_p, _fp, _fp, _fp, _fp]),
     ("dc_gb300_get_fields", C.c_int, [C.c_void_p, _fp, _fp, _fp, _fp]),
     ("dc_gb300_set_source", C.c_int, [C.c_void_p, C.c_long, _fp, C.c_int]),
@@ -419,6 +421,12 @@ class Simulation:
         a, b = np.empty(self.shape, np.float32), np.empty(self.shape, np.float32)
         check(lib().dc_gb300_get_vpz_vsv(self.h, fptr(a), fptr(b)))
         return a, b
+
+    def generate_reference(self, n, absorb: int, seed: int = 0) -> None:
+        """The reference's default medium + random velocity boundary +
+        precompute, on the GPU (sizes must be n + 2*absorb + 8)."""
+        check(lib().dc_gb300_generate_reference(self.h, int(n[0]), int(n[1]), int(n[2]),
+                                                int(absorb), int(seed)))
 
     def generate_layered(self, spec: LayeredSpec) -> None:
         check(lib().dc_gb300_generate_layered(self.h, C.byref(spec)))

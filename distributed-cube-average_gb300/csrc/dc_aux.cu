@@ -3,6 +3,8 @@
 // medium generator; plus tensor-map encoding.
 #include <cudaTypedefs.h>
 
+#include <cstdint>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -30,20 +32,6 @@ __global__ void add_value_kernel(float2 *cur, long long gi, float s) {
   v.x = __fadd_rn(v.x, s);
   v.y = __fadd_rn(v.y, s);
   cur[gi] = v;
-}
-
-__global__ void gather_kernel(const float2 *f, const long long *idx, int n,
-                              float *traces, int cap, const int *d_step,
-                              int step_offset, long long src_gi,
-                              const float *src_pre) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  const int step = *d_step + step_offset;
-  if (r >= n || step < 0 || step >= cap) return;
-  const long long i = idx[r];
-  // the source point already holds the next step's source: record the value
-  // the stencil produced, as the reference sees it after the swap
-  traces[static_cast<long long>(step) * n + r] =
-      (i == src_gi && src_pre) ? src_pre[0] : f[i].x;
 }
 
 __global__ void pack_kernel(float2 *dst, const float *p, const float *q,
@@ -177,7 +165,165 @@ __global__ void layered_kernel(const dc_gb300_layered_spec spec_v, float *coef,
   }
 }
 
+// ---- the reference medium on the GPU ------------------------------------
+// glibc's rand_r (stdlib/rand_r.c, glibc 2.39 here) advances the linear
+// congruential generator x -> 1103515245 x + 12345 (mod 2^32) three times per
+// call and returns bits 16..26, then 16..25 twice, of the three states,
+// concatenated (11 + 10 + 10 bits).  The reference's boundary sweep
+// (src/boundary.c:25-35) makes exactly one call per shell cell in global
+// z, y, x order, so the generator state before a cell's call is the seed
+// advanced by 3 * (number of shell cells before it), reached here by affine
+// skip-ahead instead of a serial sweep.
+struct Affine {
+  uint32_t a, c;  // x -> a x + c (mod 2^32)
+};
+
+__host__ __device__ __forceinline__ Affine compose(Affine f, Affine g) {  // f(g(x))
+  return Affine{f.a * g.a, f.a * g.c + f.c};
+}
+
+__host__ __device__ __forceinline__ Affine lcg_pow(unsigned long long k) {
+  Affine r{1u, 0u}, b{1103515245u, 12345u};
+  while (k) {
+    if (k & 1ull) r = compose(b, r);
+    b = compose(b, b);
+    k >>= 1;
+  }
+  return r;
+}
+
+__device__ __forceinline__ int rand_r_from(uint32_t state) {
+  uint32_t next = state * 1103515245u + 12345u;
+  int result = static_cast<int>((next >> 16) % 2048u);
+  next = next * 1103515245u + 12345u;
+  result = (result << 10) ^ static_cast<int>((next >> 16) % 1024u);
+  next = next * 1103515245u + 12345u;
+  result = (result << 10) ^ static_cast<int>((next >> 16) % 1024u);
+  return result;
+}
+
+struct RefMedium {
+  int g[3];              // cube sizes (one partition at the origin)
+  int lo[3], hi[3];      // shell box, inclusive, clipped to the cube
+  int ilo[3], ihi[3];    // interior box, inclusive
+  int first_in[3], bord_len, n[3];
+  uint32_t seed;
+  float frac, max_p, max_s;            // src/boundary.c:27-31
+  float vpz0, vsv0, eps0, delta0, theta0, phi0;  // src/precomp.c:156-169
+};
+
+__device__ __forceinline__ long long cnt_below(int v, int lo, int hi) {
+  // integers in [lo, hi] that are < v
+  if (hi < lo) return 0;
+  const long long c = static_cast<long long>(v) - lo;
+  return c < 0 ? 0 : (c > hi - lo + 1 ? hi - lo + 1 : c);
+}
+
+__device__ __forceinline__ bool in_range(int v, int lo, int hi) { return v >= lo && v <= hi; }
+
+// Shell cells strictly before (x, y, z) in the z, y, x sweep.
+__device__ long long shell_rank(const RefMedium &m, int x, int y, int z) {
+  const long long nbx = m.hi[0] >= m.lo[0] ? m.hi[0] - m.lo[0] + 1 : 0;
+  const long long nby = m.hi[1] >= m.lo[1] ? m.hi[1] - m.lo[1] + 1 : 0;
+  const long long nix = m.ihi[0] >= m.ilo[0] ? m.ihi[0] - m.ilo[0] + 1 : 0;
+  const long long niy = m.ihi[1] >= m.ilo[1] ? m.ihi[1] - m.ilo[1] + 1 : 0;
+  long long r = cnt_below(z, m.lo[2], m.hi[2]) * nbx * nby -
+                cnt_below(z, m.ilo[2], m.ihi[2]) * nix * niy;
+  if (in_range(z, m.lo[2], m.hi[2])) {
+    const bool iz = in_range(z, m.ilo[2], m.ihi[2]);
+    r += cnt_below(y, m.lo[1], m.hi[1]) * nbx - (iz ? cnt_below(y, m.ilo[1], m.ihi[1]) * nix : 0);
+    if (in_range(y, m.lo[1], m.hi[1]))
+      r += cnt_below(x, m.lo[0], m.hi[0]) -
+           ((iz && in_range(y, m.ilo[1], m.ihi[1])) ? cnt_below(x, m.ilo[0], m.ihi[0]) : 0);
+  }
+  return r;
+}
+
+__device__ __forceinline__ int shell_dist(int g, int first_in, int bord_len, int n) {
+  if (g > bord_len + n) return g - bord_len - n;
+  if (g < first_in) return first_in - g;
+  return 0;
+}
+
+__global__ void reference_medium_kernel(const RefMedium m, float *coef, float *vv,
+                                        long long pitch, long long count) {
+  const long long sx = m.g[0], sy = m.g[1], sz = m.g[2];
+  const long long n = sx * sy * sz;
+  const long long plane = pitch * sy;
+  for (long long d = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; d < n;
+       d += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int x = static_cast<int>(d % sx), y = static_cast<int>((d / sx) % sy),
+              z = static_cast<int>(d / (sx * sy));
+    float vpz = m.vpz0, vsv = m.vsv0;
+    const bool inside = in_range(x, m.ilo[0], m.ihi[0]) && in_range(y, m.ilo[1], m.ihi[1]) &&
+                        in_range(z, m.ilo[2], m.ihi[2]);
+    if (!inside) {
+      const bool shell = in_range(x, m.lo[0], m.hi[0]) && in_range(y, m.lo[1], m.hi[1]) &&
+                         in_range(z, m.lo[2], m.hi[2]);
+      if (shell) {
+        const Affine f = lcg_pow(3ull * static_cast<unsigned long long>(shell_rank(m, x, y, z)));
+        const int rv = rand_r_from(f.a * m.seed + f.c);
+        const float r = __fdiv_rn(__int2float_rn(rv), 2147483648.0f);  // RAND_MAX as float
+        int dist = shell_dist(y, m.first_in[1], m.bord_len, m.n[1]);
+        const int dz = shell_dist(z, m.first_in[2], m.bord_len, m.n[2]);
+        const int dx = shell_dist(x, m.first_in[0], m.bord_len, m.n[0]);
+        dist = dist > dz ? dist : dz;
+        dist = dist > dx ? dist : dx;
+        const float w = __fmul_rn(__int2float_rn(dist), m.frac);
+        const float omw = __fsub_rn(1.0f, w);
+        vpz = __fadd_rn(__fmul_rn(m.max_p, omw), __fmul_rn(__fmul_rn(m.max_p, r), w));
+        vsv = __fadd_rn(__fmul_rn(m.max_s, omw), __fmul_rn(__fmul_rn(m.max_s, r), w));
+      } else {
+        vpz = 0.0f;
+        vsv = 0.0f;
+      }
+    }
+    const long long pi = static_cast<long long>(z) * plane + static_cast<long long>(y) * pitch + x;
+    if (coef) {
+      float out[10];
+      precomp_point(m.theta0, m.phi0, vsv, vpz, m.eps0, m.delta0, out);
+#pragma unroll
+      for (int k = 0; k < 10; ++k) coef[k * count + pi] = out[k];
+    }
+    if (vv) {
+      vv[pi] = vpz;
+      vv[count + pi] = vsv;
+    }
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_reference_medium(cudaStream_t st, const int n[3], int absorb,
+                                    unsigned int seed, const float consts[6], float *coef,
+                                    float *vv, long long pitch, long long count) {
+  RefMedium m{};
+  const int bord = 4;  // STENCIL (include/definitions.h:4)
+  m.bord_len = bord + absorb - 1;
+  for (int d = 0; d < 3; ++d) {
+    m.n[d] = n[d];
+    m.g[d] = n[d] + 2 * absorb + 2 * bord;  // src/main.c:94-99
+    m.first_in[d] = m.bord_len + 1;
+    m.ilo[d] = m.first_in[d];
+    m.ihi[d] = std::min(m.bord_len + n[d], m.g[d] - 1);
+    m.lo[d] = bord;
+    m.hi[d] = std::min(2 * m.bord_len + n[d], m.g[d] - 1);
+  }
+  m.seed = seed;
+  m.frac = consts[0];
+  m.max_p = consts[1];
+  m.max_s = consts[2];
+  m.vpz0 = 3000.0f;
+  m.vsv0 = consts[3];
+  m.eps0 = 0.24f;
+  m.delta0 = 0.1f;
+  m.theta0 = consts[4];
+  m.phi0 = consts[5];
+  const long long total = static_cast<long long>(m.g[0]) * m.g[1] * m.g[2];
+  const int blocks = static_cast<int>(std::min<long long>((total + 255) / 256, 152 * 32));
+  reference_medium_kernel<<<blocks, 256, 0, st>>>(m, coef, vv, pitch, count);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_add_source(cudaStream_t st, float2 *cur, long long gi,
                               const float *table, int count, const int *d_step,
@@ -188,14 +334,6 @@ cudaError_t launch_add_source(cudaStream_t st, float2 *cur, long long gi,
 
 cudaError_t launch_add_value(cudaStream_t st, float2 *cur, long long gi, float value) {
   add_value_kernel<<<1, 1, 0, st>>>(cur, gi, value);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_gather(cudaStream_t st, const float2 *f, const long long *idx, int n,
-                          float *traces, int cap, const int *d_step, int step_offset,
-                          long long src_gi, const float *src_pre) {
-  gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(f, idx, n, traces, cap, d_step,
-                                                 step_offset, src_gi, src_pre);
   return cudaGetLastError();
 }
 

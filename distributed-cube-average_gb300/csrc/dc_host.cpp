@@ -137,6 +137,20 @@ extern "C" void randomVelocityBoundaryPartition(int local_sx, int local_sy, int 
       }
 }
 
+// Float constants of the reference medium, computed with the reference's
+// own expressions (src/boundary.c:27-31, src/precomp.c:156-169) so that the
+// GPU generator starts from identical values.
+extern "C" void dc_gb300_reference_medium_constants(int absorb, float out[6]) {
+  out[0] = 1.0f / static_cast<float>(absorb);           // frac
+  out[1] = 3000.0f;                                     // max_p
+  out[2] = out[1] * sqrtf(fabsf(0.24f - 0.1f) / 0.75f);  // max_s (float division)
+  const float vpz = 3000.0;
+  const float eps = 0.24, delta = 0.1;
+  out[3] = vpz * sqrtf(fabsf(eps - delta) / 0.75);      // default vsv (double division)
+  out[4] = atanf(1.0);                                  // theta
+  out[5] = 1.0;                                         // phi
+}
+
 extern "C" float dc_calculate_source(float dt, int it) {
   return source_sample(dt, it, 40.0);  // FCUT = 40 (src/calculate_source.c:5)
 }

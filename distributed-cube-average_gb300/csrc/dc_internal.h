@@ -70,10 +70,16 @@ struct StepParams {
   int src_count;
   const int *d_step;            // device step counter (graph replays)
   int step_offset;              // step = *d_step + step_offset
-  float *src_pre;               // p,q at the source point before injection
   // fused energy: sum(p^2+q^2) of the new fields, one double per step
   double *energy;
   int energy_cap;
+  // fused receivers: per (x, y) column a run [start, start + count) of
+  // receivers sorted by z (rec_z) with their trace slots (rec_r); traces
+  // are [step][nrec] p values before the next step's source
+  const int2 *rec_col;          // [sy][sx] or null
+  const int *rec_z, *rec_r;
+  float *traces;
+  int nrec, trace_cap, col_stride;
   int *err;
 };
 
@@ -98,9 +104,9 @@ struct Sim {
   float *d_src = nullptr;
   int src_count = 0;
   long long src_applied_step = -1;  // pc already holds src(step) for it
-  float *d_src_pre = nullptr;
-  // receivers
-  long long *d_rec = nullptr;
+  // receivers (see StepParams::rec_col)
+  int2 *d_rec_col = nullptr;
+  int *d_rec_z = nullptr, *d_rec_r = nullptr;
   int nrec = 0;
   float *d_traces = nullptr;
   int trace_cap = 0;
@@ -139,10 +145,6 @@ cudaError_t launch_add_source(cudaStream_t st, float2 *cur, long long gi,
                               const int *d_step, int step_offset);
 cudaError_t launch_add_value(cudaStream_t st, float2 *cur, long long gi,
                              float value);
-cudaError_t launch_gather(cudaStream_t st, const float2 *f,
-                          const long long *idx, int n, float *traces, int cap,
-                          const int *d_step, int step_offset,
-                          long long src_gi, const float *src_pre);
 // Dense (x fastest, no pitch) p and q arrays <-> pitched pair buffer; a null
 // dense pointer reads as zeros / is skipped.
 cudaError_t launch_pack(cudaStream_t st, float2 *dst, const float *p,
@@ -165,6 +167,14 @@ cudaError_t launch_precomp(cudaStream_t st, const float *theta,
 cudaError_t launch_layered(cudaStream_t st, const dc_gb300_layered_spec &spec,
                            float *coef, float *vv, long long sx, long long sy,
                            long long sz, long long pitch, long long count);
+
+// The reference's one-rank medium (default anisotropy, random velocity
+// boundary with the glibc rand_r sequence, trig precompute) generated on the
+// GPU.  consts: frac, max_p, max_s, default vsv, theta, phi -- computed on the
+// host exactly as the reference's C computes them.
+cudaError_t launch_reference_medium(cudaStream_t st, const int n[3], int absorb,
+                                    unsigned int seed, const float consts[6], float *coef,
+                                    float *vv, long long pitch, long long count);
 
 // Tensor-map encoding through the driver entry point (no -lcuda needed).
 bool encode_tiled(CUtensorMap *map, const void *base, int rank,

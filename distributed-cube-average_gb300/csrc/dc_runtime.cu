@@ -123,8 +123,9 @@ void release(Sim *s) {
   cudaFree(s->vv);
   cudaFree(s->sponge);
   cudaFree(s->d_src);
-  cudaFree(s->d_src_pre);
-  cudaFree(s->d_rec);
+  cudaFree(s->d_rec_col);
+  cudaFree(s->d_rec_z);
+  cudaFree(s->d_rec_r);
   cudaFree(s->d_traces);
   cudaFree(s->d_energy);
   cudaFree(s->d_step);
@@ -182,7 +183,6 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
   p.src_y = -1;
   p.src_z = -1;
   p.d_step = s->d_step;
-  p.src_pre = s->d_src_pre;
   p.err = s->d_err;
   return p;
 }
@@ -221,17 +221,17 @@ cudaError_t queue_step(Sim *s, int j) {
   }
   p.energy = s->d_energy;
   p.energy_cap = s->energy_cap;
+  if (s->nrec > 0) {
+    p.rec_col = s->d_rec_col;
+    p.rec_z = s->d_rec_z;
+    p.rec_r = s->d_rec_r;
+    p.traces = s->d_traces;
+    p.nrec = s->nrec;
+    p.trace_cap = s->trace_cap;
+    p.col_stride = static_cast<int>(s->sx);
+  }
   cudaError_t e = launch_pass(s, p);
   if (e != cudaSuccess) return e;
-  if (s->nrec > 0) {
-    ++s->launches;
-    const long long src_gi = s->src_gi;
-    e = launch_gather(s->stream, reinterpret_cast<const float2 *>(s->handle->abi.pp), s->d_rec,
-                      s->nrec,
-                      s->d_traces, s->trace_cap, s->d_step, j, src_gi,
-                      s->d_src_pre);
-    if (e != cudaSuccess) return e;
-  }
   swap_roles(&s->handle->abi);
   return cudaSuccess;
 }
@@ -336,8 +336,7 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
       return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of vpz/vsv failed"));
   }
   if (cudaMalloc(&s->d_step, sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&s->d_src_pre, 2 * sizeof(float)) != cudaSuccess)
+      cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess)
     return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of counters failed"));
   for (int b = 0; b < 2; ++b)
     if (cudaMemsetAsync(s->pq[b], 0, bytes * 2, s->stream) != cudaSuccess)
@@ -346,7 +345,6 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
   if (s->vv) cudaMemsetAsync(s->vv, 0, bytes * 2, s->stream);
   cudaMemsetAsync(s->d_step, 0, sizeof(int), s->stream);
   cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
-  cudaMemsetAsync(s->d_src_pre, 0, 2 * sizeof(float), s->stream);
   std::string err;
   if (s->kernel == DC_GB300_KERNEL_FAST && !fast_encode_maps(s, &err))
     return bail(fail(DC_GB300_ERR_CUDA, err));
@@ -507,6 +505,26 @@ extern "C" int dc_gb300_generate_layered(dc_gb300_sim *h, const dc_gb300_layered
   ++s->launches;
   DCG_TRY(launch_layered(s->stream, *spec, s->coef, s->vv, s->sx, s->sy, s->sz, s->pitch,
                          s->count));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" void dc_gb300_reference_medium_constants(int absorb, float out[6]);
+
+extern "C" int dc_gb300_generate_reference(dc_gb300_sim *h, long nx, long ny, long nz,
+                                           long absorb, unsigned int seed) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
+  if (nx < 1 || ny < 1 || nz < 1 || absorb < 1 || s->sx != nx + 2 * absorb + 8 ||
+      s->sy != ny + 2 * absorb + 8 || s->sz != nz + 2 * absorb + 8)
+    return fail(DC_GB300_ERR_ARG, "sizes must be n + 2*absorb + 8 per axis, absorb >= 1");
+  DCG_TRY(cudaSetDevice(s->device));
+  float consts[6];
+  dc_gb300_reference_medium_constants(static_cast<int>(absorb), consts);
+  const int n[3] = {static_cast<int>(nx), static_cast<int>(ny), static_cast<int>(nz)};
+  ++s->launches;
+  DCG_TRY(launch_reference_medium(s->stream, n, static_cast<int>(absorb), seed, consts, s->coef,
+                                  s->vv, s->pitch, s->count));
   DCG_TRY(cudaStreamSynchronize(s->stream));
   return DC_GB300_OK;
 }
@@ -751,26 +769,53 @@ extern "C" int dc_gb300_set_receivers(dc_gb300_sim *h, const long *index, int co
   DCG_TRY(cudaSetDevice(s->device));
   drop_graphs(s);
   ++s->config_version;
-  cudaFree(s->d_rec);
+  cudaFree(s->d_rec_col);
+  cudaFree(s->d_rec_z);
+  cudaFree(s->d_rec_r);
   cudaFree(s->d_traces);
-  s->d_rec = nullptr;
+  s->d_rec_col = nullptr;
+  s->d_rec_z = s->d_rec_r = nullptr;
   s->d_traces = nullptr;
   s->nrec = 0;
   s->trace_cap = 0;
   if (count <= 0) return DC_GB300_OK;
   if (!index || max_steps <= 0) return fail(DC_GB300_ERR_ARG, "receivers invalid");
-  const long long n = s->sx * s->sy * s->sz;
-  std::vector<long long> pidx(count);
+  // receivers sorted by column, then depth; each column gets its run
+  struct Rec {
+    long long col;
+    int z, r;
+  };
+  std::vector<Rec> recs(count);
   for (int r = 0; r < count; ++r) {
-    if (index[r] < 0 || index[r] >= n) return fail(DC_GB300_ERR_ARG, "receiver index out of range");
     const long long i = index[r];
     const long long x = i % s->sx, y = (i / s->sx) % s->sy, z = i / (s->sx * s->sy);
-    pidx[r] = z * s->plane + y * s->pitch + x;
+    if (i < 0 || z >= s->sz || x < 4 || x >= s->sx - 4 || y < 4 || y >= s->sy - 4 || z < 4 ||
+        z >= s->sz - 4)
+      return fail(DC_GB300_ERR_ARG, "receivers must lie in the updated region [4, s-4)^3");
+    recs[r] = Rec{y * s->sx + x, static_cast<int>(z), r};
   }
-  DCG_TRY(cudaMalloc(&s->d_rec, sizeof(long long) * count));
+  std::sort(recs.begin(), recs.end(), [](const Rec &a, const Rec &b) {
+    return a.col != b.col ? a.col < b.col : (a.z != b.z ? a.z < b.z : a.r < b.r);
+  });
+  std::vector<int2> col(static_cast<size_t>(s->sx * s->sy), make_int2(0, 0));
+  std::vector<int> rz(count), rr(count);
+  for (int k = 0; k < count; ++k) {
+    int2 &c = col[recs[k].col];
+    if (c.y == 0) c.x = k;
+    ++c.y;
+    rz[k] = recs[k].z;
+    rr[k] = recs[k].r;
+  }
+  DCG_TRY(cudaMalloc(&s->d_rec_col, sizeof(int2) * col.size()));
+  DCG_TRY(cudaMalloc(&s->d_rec_z, sizeof(int) * count));
+  DCG_TRY(cudaMalloc(&s->d_rec_r, sizeof(int) * count));
   DCG_TRY(cudaMalloc(&s->d_traces, sizeof(float) * static_cast<size_t>(count) * max_steps));
-  DCG_TRY(cudaMemcpyAsync(s->d_rec, pidx.data(), sizeof(long long) * count,
+  DCG_TRY(cudaMemcpyAsync(s->d_rec_col, col.data(), sizeof(int2) * col.size(),
                           cudaMemcpyHostToDevice, s->stream));
+  DCG_TRY(cudaMemcpyAsync(s->d_rec_z, rz.data(), sizeof(int) * count, cudaMemcpyHostToDevice,
+                          s->stream));
+  DCG_TRY(cudaMemcpyAsync(s->d_rec_r, rr.data(), sizeof(int) * count, cudaMemcpyHostToDevice,
+                          s->stream));
   DCG_TRY(cudaMemsetAsync(s->d_traces, 0, sizeof(float) * static_cast<size_t>(count) * max_steps,
                           s->stream));
   s->nrec = count;
@@ -845,7 +890,7 @@ int capture_chunk(Sim *s, cudaGraphExec_t *out) {
   return DC_GB300_OK;
 }
 
-long long launches_per_step(const Sim *s) { return 1 + (s->nrec > 0 ? 1 : 0); }
+long long launches_per_step(const Sim *) { return 1; }
 
 }  // namespace
 

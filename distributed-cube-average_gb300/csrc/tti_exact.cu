@@ -110,6 +110,14 @@ __global__ void __launch_bounds__(128)
   const int ze = min(zb + prm.zchunk, prm.z1);
   const long long sY = prm.pitch, sZ = prm.plane;
   float e_acc = 0.f;
+  int rk = 0, rend = 0, rnext = -1;  // receivers of this column
+  if (prm.rec_col) {
+    const int2 e = prm.rec_col[gy * prm.col_stride + gx];
+    rk = e.x;
+    rend = e.x + e.y;
+    while (rk < rend && prm.rec_z[rk] < zb) ++rk;
+    rnext = rk < rend ? prm.rec_z[rk] : -1;
+  }
   for (int z = zb; z < ze; ++z) {
     const long long i = static_cast<long long>(z) * sZ +
                         static_cast<long long>(gy) * sY + gx;
@@ -173,11 +181,18 @@ __global__ void __launch_bounds__(128)
       nq = __fadd_rn(__fsub_rn(__fmul_rn(2.0f, qc), qpo), tq);
     }
     if (prm.energy) e_acc = fmaf(np, np, fmaf(nq, nq, e_acc));
+    if (z == rnext) {
+      const int step = *prm.d_step + prm.step_offset;
+      do {
+        if (step >= 0 && step < prm.trace_cap)
+          prm.traces[static_cast<long long>(step) * prm.nrec + prm.rec_r[rk]] = np;
+        ++rk;
+      } while (rk < rend && prm.rec_z[rk] == z);
+      rnext = rk < rend ? prm.rec_z[rk] : -1;
+    }
     if (gx == prm.src_x && gy == prm.src_y && z == prm.src_z) {
       const int step = *prm.d_step + prm.step_offset;
       const float sv = step + 1 < prm.src_count ? prm.src_table[step + 1] : 0.0f;
-      prm.src_pre[0] = np;
-      prm.src_pre[1] = nq;
       np = __fadd_rn(np, sv);
       nq = __fadd_rn(nq, sv);
     }

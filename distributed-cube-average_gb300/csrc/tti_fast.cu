@@ -190,6 +190,15 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
                         ? prm.sponge[gx] * prm.sponge[prm.sponge_oy + gy]
                         : 1.0f;
   const bool src_col = active && gx == prm.src_x && gy == prm.src_y;
+  // receivers of this column at or below the first output plane
+  int rk = 0, rend = 0, rnext = -1;
+  if (prm.rec_col && active) {
+    const int2 e = prm.rec_col[gy * prm.col_stride + gx];
+    rk = e.x;
+    rend = e.x + e.y;
+    while (rk < rend && prm.rec_z[rk] < zb) ++rk;
+    rnext = rk < rend ? prm.rec_z[rk] : -1;
+  }
   const int c0 = (ty + kHalo) * HX + tx + kHalo;  // centre in a halo plane
   const int od = ty * HX + tx + kHalo;            // centre in a dy plane
   const int ot = ty * TX + tx;                    // centre in a tile
@@ -320,12 +329,20 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
           }
           if (active) {
             if (prm.energy) e_acc = fma2(nv, nv, e_acc);
-            if (src_col && zb + it - 2 * kHalo == prm.src_z) {
+            const int z = zb + it - 2 * kHalo;
+            if (z == rnext) {
+              const int step = *prm.d_step + prm.step_offset;
+              do {
+                if (step >= 0 && step < prm.trace_cap)
+                  prm.traces[static_cast<long long>(step) * prm.nrec + prm.rec_r[rk]] = nv.x;
+                ++rk;
+              } while (rk < rend && prm.rec_z[rk] == z);
+              rnext = rk < rend ? prm.rec_z[rk] : -1;
+            }
+            if (src_col && z == prm.src_z) {
               const int step = *prm.d_step + prm.step_offset;
               const float sv =
                   step + 1 < prm.src_count ? prm.src_table[step + 1] : 0.0f;
-              prm.src_pre[0] = nv.x;
-              prm.src_pre[1] = nv.y;
               nv.x += sv;
               nv.y += sv;
             }

@@ -246,6 +246,14 @@ int dc_gb300_set_anisotropy(dc_gb300_sim *sim, const dc_anisotropy_t *host);
 int dc_gb300_get_precomp(dc_gb300_sim *sim, const dc_precomp_vars *host);
 int dc_gb300_get_vpz_vsv(dc_gb300_sim *sim, float *vpz, float *vsv);
 
+/* The reference's one-rank medium generated on the GPU: the default
+ * anisotropy (src/precomp.c:156-169), the random velocity boundary of
+ * src/boundary.c:7-104 with the same glibc rand_r sequence (replayed by
+ * skip-ahead, not a serial sweep) and the FP64 trig precompute.  The
+ * simulation's sizes must be n + 2*absorb + 8 per axis (src/main.c:94-99). */
+int dc_gb300_generate_reference(dc_gb300_sim *sim, long nx, long ny, long nz,
+                                long absorb, unsigned int seed);
+
 /* Seeded layered medium generated on the GPU (see dc_gb300_layered_spec). */
 #define DC_GB300_MAX_LAYERS 32
 #define DC_GB300_MAX_FEATURES 128

@@ -11,6 +11,7 @@
 #include "dc_oracle.h"
 
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -386,6 +387,36 @@ void o_sponge_profile(long s, long a, double kappa, float *g) {
   }
 }
 
+float o_round_f16(float x) {
+  /* IEEE binary16, round to nearest even (GCC's _Float16 conversion) */
+  return (float)(_Float16)x;
+}
+
+float o_round_bf16(float x) {
+  /* bfloat16: keep the top 16 bits, round to nearest even; NaN stays NaN */
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;
+  u += 0x7fffu + ((u >> 16) & 1u);
+  u &= 0xffff0000u;
+  float r;
+  memcpy(&r, &u, 4);
+  return r;
+}
+
+static void round_store(const o_run_cfg *cfg, float *f, int comp) {
+  const long sx = cfg->sx, sy = cfg->sy, sz = cfg->sz;
+  const float sc = ldexpf(1.0f, cfg->store_exp[comp]);
+  const float inv = ldexpf(1.0f, -cfg->store_exp[comp]);
+  for (long z = 4; z < sz - 4; ++z)
+    for (long y = 4; y < sy - 4; ++y)
+      for (long x = 4; x < sx - 4; ++x) {
+        const long i = x + y * sx + z * sx * sy;
+        const float v = f[i] * sc;
+        f[i] = (cfg->store == O_STORE_F16 ? o_round_f16(v) : o_round_bf16(v)) * inv;
+      }
+}
+
 /* ---- time loop ----------------------------------------------------------- */
 
 static void swap_ptr(void **a, void **b) {
@@ -419,6 +450,10 @@ int o_run(const o_run_cfg *cfg, void *pp0, void *pc0, void *qp0, void *qc0) {
                cfg->dt, pc, qc, pp, qp, cfg->coef, cfg->vpz, cfg->vsv, sp,
                cfg->nthreads) != 0)
       return -1;
+    if (!f64 && cfg->store != O_STORE_F32) {
+      round_store(cfg, (float *)pp, 0);
+      round_store(cfg, (float *)qp, 1);
+    }
     /* src/worker.c:506 */
     swap_ptr(&pp, &pc);
     swap_ptr(&qp, &qc);

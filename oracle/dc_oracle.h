@@ -100,7 +100,18 @@ typedef struct {
   double *traces;                /* [steps*nrec] or NULL */
   double *energy;                /* [steps]: sum(p^2+q^2) over [4,s-4)^3 */
   int nthreads;
+  /* Mixed-precision storage emulation (this library's own form, not the
+   * reference's): after each step every updated pp/qp value is rounded to
+   * `store` (O_STORE_*) after scaling by 2^store_exp[0] (p) / [1] (q). */
+  int store;
+  int store_exp[2];
 } o_run_cfg;
+
+enum { O_STORE_F32 = 0, O_STORE_F16 = 1, O_STORE_BF16 = 2 };
+
+/* Round-to-nearest-even of x to FP16 / BF16, returned as float. */
+float o_round_f16(float x);
+float o_round_bf16(float x);
 
 /* One-rank replay of dc_worker_process (src/worker.c:466-511): per step
  * add source to pc and qc, update [4,s-4)^3, swap.  On return pc/qc hold the

@@ -23,6 +23,7 @@ NCOEF = 10
 COEF_NAMES = ("ch1dxx", "ch1dyy", "ch1dzz", "ch1dxy", "ch1dyz", "ch1dxz",
               "v2px", "v2pz", "v2sz", "v2pn")
 KIND_F32, KIND_F32_REFCUDA, KIND_F64 = 0, 1, 2
+STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 
 _fp = C.POINTER(C.c_float)
 _dp = C.POINTER(C.c_double)
@@ -57,6 +58,8 @@ class _RunCfg(C.Structure):
         ("traces", _dp),
         ("energy", _dp),
         ("nthreads", C.c_int),
+        ("store", C.c_int),
+        ("store_exp", C.c_int * 2),
     ]
 
 
@@ -147,7 +150,8 @@ class Port:
             raise ValueError("box outside the compute region")
 
     def run(self, kind, sizes, d, dt, steps, pp, pc, qp, qc, coef=None, vpz=None, vsv=None,
-            src_index=-1, src=None, sponge=None, rec=None, energy=False, nthreads=None) -> RunResult:
+            src_index=-1, src=None, sponge=None, rec=None, energy=False, nthreads=None,
+            store=0, store_exp=(0, 0)) -> RunResult:
         """Time loop; field arrays are updated in place (copies are the
         caller's business).  Returns the final fields and optional
         traces [steps, nrec] and energy [steps]."""
@@ -184,6 +188,8 @@ class Port:
             en = np.zeros(steps, np.float64)
             cfg.energy = en.ctypes.data_as(_dp)
         cfg.nthreads = nthreads or default_threads()
+        cfg.store = store
+        cfg.store_exp[0], cfg.store_exp[1] = store_exp
         rc = self.lib.o_run(C.byref(cfg), _vp(pp), _vp(pc), _vp(qp), _vp(qc))
         if rc != 0:
             raise RuntimeError("oracle run failed")

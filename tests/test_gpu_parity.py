@@ -305,3 +305,50 @@ def test_halo_face_roundtrip(dc):
     back = dc.extract_halo_face(data, start, end, sizes, view.pp)
     assert np.array_equal(back, buf)
     dc.device_data_free(data)
+
+
+@pytest.mark.parametrize("n,absorb,seed", [((12, 10, 9), 3, 0), ((40, 7, 19), 5, 123),
+                                           ((64, 64, 64), 16, 0)])
+def test_reference_medium_generated_on_gpu(dc, port, n, absorb, seed):
+    """Default anisotropy + random velocity boundary (glibc rand_r sequence
+    replayed by skip-ahead) + FP64 precompute, all on the GPU, against the
+    host restatement pinned to the reference."""
+    geom = Geometry(n, absorb)
+    aniso, coef = reference_medium(port, geom, seed=seed)
+    with dc.Simulation(geom.sizes, device=0) as sim:
+        sim.generate_reference(n, absorb, seed)
+        got = sim.get_precomp()
+    for k in range(10):
+        assert np.array_equal(got[k], coef[k]), k
+    with dc.Simulation(geom.sizes, device=0, medium=dc.MEDIUM_VPZ_VSV) as sim:
+        sim.generate_reference(n, absorb, seed)
+        vpz, vsv = sim.get_vpz_vsv()
+    assert np.array_equal(vpz, aniso["vpz"]) and np.array_equal(vsv, aniso["vsv"])
+
+
+@pytest.mark.parametrize("kernel", [1, 0])
+def test_receiver_columns_and_duplicates(dc, port, kernel):
+    """Several receivers in one column (a vertical array, spanning the
+    kernel's z-chunks), duplicated indices and scattered points."""
+    geom = Geometry((20, 18, 70), 4)
+    aniso, coef = reference_medium(port, geom)
+    steps, dt = 40, 1e-3
+    src = port.source_table(dt, steps)
+    sx, sy, sz = geom.sizes
+    cx, cy = sx // 2 + 2, sy // 2 - 1
+    rec = [geom.index(cx, cy, z) for z in range(4, sz - 4, 5)]
+    rec += [rec[3], geom.index(5, 6, 7), geom.index(sx - 5, sy - 5, sz - 5), geom.source_index]
+    ref = port.run(KIND_F32, geom.sizes, (12.5,) * 3, dt, steps, *zeros(geom.shape), coef=coef,
+                   src_index=geom.source_index, src=src, rec=rec)
+    with dc.Simulation(geom.sizes, (12.5,) * 3, dt, kernel=kernel, device=0) as sim:
+        sim.set_precomp(coef)
+        sim.set_fields()
+        sim.set_source(geom.source_index, src)
+        sim.set_receivers(rec, steps)
+        sim.run(steps)
+        sim.synchronize()
+        tr = sim.traces(steps)
+    if kernel == 1:
+        assert np.array_equal(tr, ref.traces.astype(np.float32))
+    else:
+        assert rel_l2(tr, ref.traces) <= 1e-5
