@@ -69,6 +69,7 @@ struct StepParams {
   const float *src_table;
   int src_count;
   const int *d_step;            // device step counter (graph replays)
+  float *src_pre;               // (p, q) at the source point before injection
   int step_offset;              // step = *d_step + step_offset
   // fused energy: sum(p^2+q^2) of the new fields, one double per step
   double *energy;
@@ -104,6 +105,7 @@ struct Sim {
   float *d_src = nullptr;
   int src_count = 0;
   long long src_applied_step = -1;  // pc already holds src(step) for it
+  float *d_src_pre = nullptr;       // values the stencil stored before that
   // receivers (see StepParams::rec_col)
   int2 *d_rec_col = nullptr;
   int *d_rec_z = nullptr, *d_rec_r = nullptr;

@@ -123,6 +123,7 @@ void release(Sim *s) {
   cudaFree(s->vv);
   cudaFree(s->sponge);
   cudaFree(s->d_src);
+  cudaFree(s->d_src_pre);
   cudaFree(s->d_rec_col);
   cudaFree(s->d_rec_z);
   cudaFree(s->d_rec_r);
@@ -183,6 +184,7 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
   p.src_y = -1;
   p.src_z = -1;
   p.d_step = s->d_step;
+  p.src_pre = s->d_src_pre;
   p.err = s->d_err;
   return p;
 }
@@ -234,6 +236,33 @@ cudaError_t queue_step(Sim *s, int j) {
   if (e != cudaSuccess) return e;
   swap_roles(&s->handle->abi);
   return cudaSuccess;
+}
+
+// After a run the source point of pc/qc already holds the next step's
+// amplitude (fused into the last store); the reference adds it only at the
+// start of the next step.  The values before that addition are kept in
+// d_src_pre so every observable state is the reference's.
+bool source_pending(const Sim *s) {
+  return s->src_gi >= 0 && s->steps_done > 0 && s->src_applied_step == s->steps_done;
+}
+
+// Puts the pre-injection values back into the device field and marks the
+// source of the current step as not applied (the next run re-adds it).
+cudaError_t settle_source(Sim *s) {
+  if (!source_pending(s)) return cudaSuccess;
+  int cur = -1, prev = -1;
+  roles(s, &cur, &prev);
+  cudaError_t e = cudaMemcpyAsync(s->pq[cur] + s->src_gi, s->d_src_pre, sizeof(float2),
+                                  cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) s->src_applied_step = -1;
+  return e;
+}
+
+// Dense index of the source point (for patching host copies).
+long long source_dense(const Sim *s) {
+  const long long z = s->src_gi / s->plane, r = s->src_gi % s->plane;
+  const long long y = r / s->pitch, x = r % s->pitch;
+  return x + y * s->sx + z * s->sx * s->sy;
 }
 
 int check_err_word(Sim *s) {
@@ -336,7 +365,8 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
       return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of vpz/vsv failed"));
   }
   if (cudaMalloc(&s->d_step, sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess)
+      cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->d_src_pre, 2 * sizeof(float)) != cudaSuccess)
     return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of counters failed"));
   for (int b = 0; b < 2; ++b)
     if (cudaMemsetAsync(s->pq[b], 0, bytes * 2, s->stream) != cudaSuccess)
@@ -345,6 +375,7 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
   if (s->vv) cudaMemsetAsync(s->vv, 0, bytes * 2, s->stream);
   cudaMemsetAsync(s->d_step, 0, sizeof(int), s->stream);
   cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
+  cudaMemsetAsync(s->d_src_pre, 0, 2 * sizeof(float), s->stream);
   std::string err;
   if (s->kernel == DC_GB300_KERNEL_FAST && !fast_encode_maps(s, &err))
     return bail(fail(DC_GB300_ERR_CUDA, err));
@@ -592,7 +623,16 @@ extern "C" int dc_gb300_get_fields(dc_gb300_sim *h, float *pp, float *pc, float 
                               s->stream));
   }
   DCG_TRY(cudaFreeAsync(stage, s->stream));
+  float pre[2] = {0.f, 0.f};
+  const bool patch = source_pending(s) && (pc || qc);
+  if (patch)
+    DCG_TRY(cudaMemcpyAsync(pre, s->d_src_pre, sizeof(pre), cudaMemcpyDeviceToHost, s->stream));
   DCG_TRY(cudaStreamSynchronize(s->stream));
+  if (patch) {
+    const long long i = source_dense(s);
+    if (pc) pc[i] = pre[0];
+    if (qc) qc[i] = pre[1];
+  }
   return DC_GB300_OK;
 }
 
@@ -628,7 +668,13 @@ extern "C" int dc_gb300_save_checkpoint(dc_gb300_sim *h, const char *path) {
   hd.sy = s->sy;
   hd.sz = s->sz;
   hd.steps_done = s->steps_done;
-  hd.src_applied = (s->src_gi >= 0 && s->src_applied_step == s->steps_done) ? 1 : 0;
+  hd.src_applied = 0;  // the file holds the reference's state (no pending source)
+  float pre[2] = {0.f, 0.f};
+  const bool patch = source_pending(s);
+  if (patch) {
+    DCG_TRY(cudaMemcpyAsync(pre, s->d_src_pre, sizeof(pre), cudaMemcpyDeviceToHost, s->stream));
+    DCG_TRY(cudaStreamSynchronize(s->stream));
+  }
   bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1;
   for (int b : {prev, cur}) {
     if (!ok) break;
@@ -642,6 +688,11 @@ extern "C" int dc_gb300_save_checkpoint(dc_gb300_sim *h, const char *path) {
       std::fclose(f);
       cudaFreeAsync(stage, s->stream);
       return fail(DC_GB300_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (patch && b == cur) {
+      const long long i = source_dense(s);
+      host[i] = pre[0];
+      host[n + i] = pre[1];
     }
     ok = std::fwrite(host.data(), sizeof(float), host.size(), f) == host.size();
   }
@@ -708,6 +759,7 @@ extern "C" int dc_gb300_set_source(dc_gb300_sim *h, long index, const float *amp
   Sim *s = impl(h);
   if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
   DCG_TRY(cudaSetDevice(s->device));
+  DCG_TRY(settle_source(s));  // the old source's pending amplitude comes out first
   drop_graphs(s);
   ++s->config_version;
   if (index < 0) {

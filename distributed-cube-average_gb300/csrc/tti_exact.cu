@@ -193,6 +193,8 @@ __global__ void __launch_bounds__(128)
     if (gx == prm.src_x && gy == prm.src_y && z == prm.src_z) {
       const int step = *prm.d_step + prm.step_offset;
       const float sv = step + 1 < prm.src_count ? prm.src_table[step + 1] : 0.0f;
+      prm.src_pre[0] = np;
+      prm.src_pre[1] = nq;
       np = __fadd_rn(np, sv);
       nq = __fadd_rn(nq, sv);
     }

@@ -343,6 +343,8 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
               const int step = *prm.d_step + prm.step_offset;
               const float sv =
                   step + 1 < prm.src_count ? prm.src_table[step + 1] : 0.0f;
+              prm.src_pre[0] = nv.x;
+              prm.src_pre[1] = nv.y;
               nv.x += sv;
               nv.y += sv;
             }

@@ -289,7 +289,10 @@ int dc_gb300_get_fields(dc_gb300_sim *sim, float *pp, float *pc, float *qp,
 
 /* Point source at linear index `index`: before step it, amplitudes[it] is
  * added to pc and qc (src/worker.c:467-470); steps beyond `count` add 0.
- * index < 0 removes the source. */
+ * index < 0 removes the source.  The addition for step it+1 is fused into
+ * the store of step it; the fields returned by dc_gb300_get_fields and saved
+ * by checkpoints are nevertheless exactly the reference's state after the
+ * steps run (without the next step's amplitude). */
 int dc_gb300_set_source(dc_gb300_sim *sim, long index,
                         const float *amplitudes, int count);
 

@@ -352,3 +352,39 @@ def test_receiver_columns_and_duplicates(dc, port, kernel):
         assert np.array_equal(tr, ref.traces.astype(np.float32))
     else:
         assert rel_l2(tr, ref.traces) <= 1e-5
+
+
+@pytest.mark.parametrize("kernel", [1, 0])
+def test_observed_state_excludes_next_source(dc, port, kernel):
+    """The next step's amplitude is fused into the store, yet get_fields after
+    run(N) is the reference's state after N steps even when the amplitude
+    table is longer; replacing the source between runs keeps that too."""
+    geom = Geometry((16, 14, 12), 3)
+    aniso, coef = reference_medium(port, geom)
+    dt = 1e-3
+    long_src = port.source_table(dt, 200)
+    other = geom.index(geom.sizes[0] // 2 - 3, geom.sizes[1] // 2, geom.sizes[2] // 2 + 2)
+    # oracle: 30 steps with the centre source, then 25 with `other`
+    z = zeros(geom.shape)
+    ref1 = port.run(KIND_F32, geom.sizes, (12.5,) * 3, dt, 30, *z, coef=coef,
+                    src_index=geom.source_index, src=long_src)
+    src2 = np.concatenate([np.zeros(30, np.float32), long_src[30:55]])
+    # continue from ref1's state: pp<-ref1.pp etc. (o_run leaves pc = current)
+    ref2 = port.run(KIND_F32, geom.sizes, (12.5,) * 3, dt, 25, ref1.pp.copy(), ref1.pc.copy(),
+                    ref1.qp.copy(), ref1.qc.copy(), coef=coef, src_index=other,
+                    src=long_src[30:55])
+    tol = 0.0 if kernel == 1 else 1e-5
+    with dc.Simulation(geom.sizes, (12.5,) * 3, dt, kernel=kernel, device=0) as sim:
+        sim.set_precomp(coef)
+        sim.set_fields()
+        sim.set_source(geom.source_index, long_src)
+        sim.run(30)
+        sim.synchronize()
+        f = sim.get_fields()
+        assert rel_l2(f["pc"], ref1.pc) <= tol and rel_l2(f["qc"], ref1.qc) <= tol
+        assert rel_l2(f["pp"], ref1.pp) <= tol
+        sim.set_source(other, src2)
+        sim.run(25)
+        sim.synchronize()
+        f = sim.get_fields()
+        assert rel_l2(f["pc"], ref2.pc) <= tol and rel_l2(f["qc"], ref2.qc) <= tol
