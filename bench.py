@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--kernel", choices=("fast", "exact"), default="fast")
+    ap.add_argument("--medium", choices=("f32", "f16", "bf16"), default="f32",
+                    help="coefficient storage read by the fast kernel")
     ap.add_argument("--n", type=int, default=N_INTERIOR, help="interior cells per axis")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -290,7 +292,10 @@ def run_ours(args, rank, world, local):
     sponge = [dc.sponge_profile(s, geom.absorb, SPONGE_KAPPA) for s in sizes]
 
     # ---- device-resident run (value, roofline) -------------------------
-    sim = dc.Simulation(sizes, (DX,) * 3, DT, kernel=kernel, medium=dc.MEDIUM_PRECOMP,
+    medium_form = {"f32": dc.MEDIUM_PRECOMP, "f16": dc.MEDIUM_PRECOMP_F16,
+                   "bf16": dc.MEDIUM_PRECOMP_BF16}[args.medium]
+    bytes_per_update = BYTES_PER_UPDATE if args.medium == "f32" else 44
+    sim = dc.Simulation(sizes, (DX,) * 3, DT, kernel=kernel, medium=medium_form,
                         device=local)
     sim.generate_layered(make_spec(geom))
     sim.set_fields()
@@ -315,10 +320,11 @@ def run_ours(args, rank, world, local):
     barrier()
     value = pts * args.steps * world / (ms * 1e-3) / 1e9
     stencil_ms = ms / args.steps  # graph-replayed region: one stencil launch per step
-    achieved = BYTES_PER_UPDATE * pts / (stencil_ms * 1e-3) / 1e9
+    achieved = bytes_per_update * pts / (stencil_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
     traffic_pp = (profiled_traffic("tti_fast_config2.md")
-                  if kernel == dc.KERNEL_FAST and args.n == N_INTERIOR else None)
+                  if kernel == dc.KERNEL_FAST and args.n == N_INTERIOR and args.medium == "f32"
+                  else None)
     out_fields = sim.get_fields() if not args.no_cpu_baseline else None
     sim.close()
 
@@ -351,12 +357,13 @@ def run_ours(args, rank, world, local):
         "data": "synthetic (seeded 12-layer TTI medium, numpy PCG64 seed 2026, generated on GPU)",
         "config": {"workload": f"plain FP32 TTI, {args.n}^3 interior + {ABSORB}-cell sponge, "
                                f"{geom.sizes[0]}^3 padded, dt 0.8 ms, 20 Hz Ricker",
-                   "kernel": args.kernel, "points_per_step": pts, "global_batch": world,
+                   "kernel": args.kernel, "medium_storage": args.medium,
+                   "points_per_step": pts, "global_batch": world,
                    "seq_len": None, "parallelism": f"shots{world}" if world > 1 else "single",
                    "l2": "inputs 13 GB >> 129 MB L2; no flush"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "bytes_per_update": BYTES_PER_UPDATE,
+                     "bytes_per_update": bytes_per_update,
                      "traffic": (traffic_pp * pts) if traffic_pp else None},
         "cpu_baseline": cpu,
         "e2e": e2e,

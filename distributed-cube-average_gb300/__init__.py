@@ -30,7 +30,7 @@ HEADER = PKG_DIR.parent / "include" / "dc_gb300.h"
 
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_DEVICE, ERR_TIMEOUT, ERR_STATE = range(7)
 KERNEL_FAST, KERNEL_EXACT = 0, 1
-MEDIUM_PRECOMP, MEDIUM_VPZ_VSV = 0, 1
+MEDIUM_PRECOMP, MEDIUM_VPZ_VSV, MEDIUM_PRECOMP_F16, MEDIUM_PRECOMP_BF16 = 0, 1, 2, 3
 MAX_LAYERS, MAX_FEATURES = 32, 128
 
 # dc_precomp_vars field order (include/precomp.h:6-17)

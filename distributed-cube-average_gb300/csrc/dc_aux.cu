@@ -1,6 +1,8 @@
 // dc_aux.cu -- small kernels around the stencil: source injection, receiver
 // gather, step counter, the FP64 medium precompute and the seeded layered
 // medium generator; plus tensor-map encoding.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
 #include <cstdint>
@@ -110,7 +112,7 @@ __global__ void precomp_kernel(const float *theta, const float *phi,
     float out[10];
     precomp_point(theta[d], phi[d], vsv[d], vpz[d], eps[d], delta[d], out);
 #pragma unroll
-    for (int k = 0; k < 10; ++k) coef[k * count + d] = out[k];
+    for (int k = 0; k < 10; ++k) coef[coef_index(k, d, count)] = out[k];
   }
 }
 
@@ -156,11 +158,11 @@ __global__ void layered_kernel(const dc_gb300_layered_spec spec_v, float *coef,
       float out[10];
       precomp_point(theta, phi, vs, vp, e, dl, out);
 #pragma unroll
-      for (int k = 0; k < 10; ++k) coef[k * count + pi] = out[k];
+      for (int k = 0; k < 10; ++k) coef[coef_index(k, pi, count)] = out[k];
     }
     if (vv) {
-      vv[pi] = vp;
-      vv[count + pi] = vs;
+      vv[2 * pi] = vp;
+      vv[2 * pi + 1] = vs;
     }
   }
 }
@@ -283,16 +285,124 @@ __global__ void reference_medium_kernel(const RefMedium m, float *coef, float *v
       float out[10];
       precomp_point(m.theta0, m.phi0, vsv, vpz, m.eps0, m.delta0, out);
 #pragma unroll
-      for (int k = 0; k < 10; ++k) coef[k * count + pi] = out[k];
+      for (int k = 0; k < 10; ++k) coef[coef_index(k, pi, count)] = out[k];
     }
     if (vv) {
-      vv[pi] = vpz;
-      vv[count + pi] = vsv;
+      vv[2 * pi] = vpz;
+      vv[2 * pi + 1] = vsv;
     }
   }
 }
 
+// One coefficient (DevCoef k): dense array <-> grouped pitched layout.
+__global__ void coef_component_kernel(float *coef, float *dense, int k, long long sx,
+                                      long long n, long long pitch, long long count,
+                                      bool to_grouped) {
+  for (long long d = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; d < n;
+       d += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long x = d % sx, yz = d / sx;
+    float *g = coef + coef_index(k, yz * pitch + x, count);
+    if (to_grouped)
+      *g = dense[d];
+    else
+      dense[d] = *g;
+  }
+}
+
+// max |v| over the four velocity terms, as float bits (non-negative floats
+// order like their bit patterns)
+__global__ void coef_vmax_kernel(const float *coef, long long count, unsigned int *out) {
+  unsigned int m = 0;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const float4 g1 = reinterpret_cast<const float4 *>(coef + 4 * count)[i];
+    const float2 g2 = reinterpret_cast<const float2 *>(coef + 8 * count)[i];
+    const float v = fmaxf(fmaxf(fabsf(g1.z), fabsf(g1.w)), fmaxf(fabsf(g2.x), fabsf(g2.y)));
+    m = max(m, __float_as_uint(v));
+  }
+  for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void coef_repitch_kernel(float *coef, const float *gd, long long sx, long long sy,
+                                    long long n, long long pitch, long long count) {
+  for (long long d = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; d < n;
+       d += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long x = d % sx, yz = d / sx;
+    const long long pi = yz * pitch + x;
+#pragma unroll
+    for (int k = 0; k < 10; ++k) coef[coef_index(k, pi, count)] = gd[coef_index(k, d, n)];
+  }
+}
+
+template <typename H2>
+__device__ __forceinline__ H2 to_h2(float a, float b);
+template <>
+__device__ __forceinline__ __half2 to_h2<__half2>(float a, float b) {
+  return __floats2half2_rn(a, b);
+}
+template <>
+__device__ __forceinline__ __nv_bfloat162 to_h2<__nv_bfloat162>(float a, float b) {
+  return __floats2bfloat162_rn(a, b);
+}
+
+template <typename H2>
+__global__ void coef_narrow_kernel(const float *coef, H2 *h0, H2 *h1, float vscale,
+                                   long long count) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const float4 g0 = reinterpret_cast<const float4 *>(coef)[i];
+    const float4 g1 = reinterpret_cast<const float4 *>(coef + 4 * count)[i];
+    const float2 g2 = reinterpret_cast<const float2 *>(coef + 8 * count)[i];
+    h0[4 * i + 0] = to_h2<H2>(g0.x, g0.y);  // cxx, cyy
+    h0[4 * i + 1] = to_h2<H2>(g0.z, g0.w);  // cxy, czz
+    h0[4 * i + 2] = to_h2<H2>(g1.x, g1.y);  // cxz, cyz
+    h0[4 * i + 3] = to_h2<H2>(g1.z * vscale, g1.w * vscale);  // v2px, v2pz
+    h1[i] = to_h2<H2>(g2.x * vscale, g2.y * vscale);          // v2sz, v2pn
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_coef_component(cudaStream_t st, float *coef, float *dense, int k,
+                                  long long sx, long long sy, long long sz, long long pitch,
+                                  long long count, bool to_grouped) {
+  const long long n = sx * sy * sz;
+  const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 32)));
+  coef_component_kernel<<<blocks, 256, 0, st>>>(coef, dense, k, sx, n, pitch, count, to_grouped);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coef_vmax(cudaStream_t st, const float *coef, long long count,
+                             unsigned int *out) {
+  const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((count + 255) / 256, 152 * 16)));
+  coef_vmax_kernel<<<blocks, 256, 0, st>>>(coef, count, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coef_repitch(cudaStream_t st, float *coef, const float *grouped_dense,
+                                long long sx, long long sy, long long sz, long long pitch,
+                                long long count) {
+  const long long n = sx * sy * sz;
+  const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 32)));
+  coef_repitch_kernel<<<blocks, 256, 0, st>>>(coef, grouped_dense, sx, sy, n, pitch, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coef_narrow(cudaStream_t st, const float *coef, void *coef16, int form,
+                               int vexp, long long count) {
+  const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((count + 255) / 256, 152 * 32)));
+  const float vscale = ldexpf(1.0f, -vexp);
+  if (form == CF_F16) {
+    __half2 *h0 = static_cast<__half2 *>(coef16);
+    coef_narrow_kernel<__half2><<<blocks, 256, 0, st>>>(coef, h0, h0 + 4 * count, vscale, count);
+  } else {
+    __nv_bfloat162 *h0 = static_cast<__nv_bfloat162 *>(coef16);
+    coef_narrow_kernel<__nv_bfloat162><<<blocks, 256, 0, st>>>(coef, h0, h0 + 4 * count, vscale,
+                                                               count);
+  }
+  return cudaGetLastError();
+}
 
 cudaError_t launch_reference_medium(cudaStream_t st, const int n[3], int absorb,
                                     unsigned int seed, const float consts[6], float *coef,
@@ -394,7 +504,7 @@ cudaError_t launch_layered(cudaStream_t st, const dc_gb300_layered_spec &spec,
 
 bool encode_tiled(CUtensorMap *map, const void *base, int rank,
                   const uint64_t *dims, const uint64_t *strides_bytes,
-                  const uint32_t *box, std::string *err, bool pairs) {
+                  const uint32_t *box, std::string *err, CUtensorMapDataType dt) {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
   static cudaError_t lookup_err = cudaSuccess;
@@ -411,9 +521,6 @@ bool encode_tiled(CUtensorMap *map, const void *base, int rank,
     return false;
   }
   cuuint32_t elem_strides[5] = {1, 1, 1, 1, 1};
-  // (p, q) pairs travel as opaque 8-byte elements
-  const CUtensorMapDataType dt =
-      pairs ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
   CUresult r = fn(map, dt, rank, const_cast<void *>(base),
                   dims, strides_bytes, box, elem_strides, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,

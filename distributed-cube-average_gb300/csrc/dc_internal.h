@@ -27,13 +27,27 @@ namespace dcg {
 #define DCG_L3 (4.0f / 105.0f)
 #define DCG_L4 (-1.0f / 280.0f)
 
-// Order of the coefficient arrays inside the device medium block.  The
-// three in-plane coefficients come first so one TMA box fetches them at the
-// leading plane and a second box the other seven at the output plane.
+// The ten medium coefficients of a point are stored grouped, so one thread
+// reads all of them with three vector loads:
+//   G0 float4 (cxx, cyy, cxy, czz)   at coef[4*i .. 4*i+3]
+//   G1 float4 (cxz, cyz, v2px, v2pz) at coef[4*count + 4*i ..]
+//   G2 float2 (v2sz, v2pn)           at coef[8*count + 2*i ..]
+// (count = padded points).  DevCoef numbers the coefficients in that order.
 enum DevCoef {
   DC_CXX = 0, DC_CYY, DC_CXY, DC_CZZ, DC_CXZ, DC_CYZ,
   DC_V2PX, DC_V2PZ, DC_V2SZ, DC_V2PN, DC_NCOEF
 };
+
+__host__ __device__ __forceinline__ long long coef_index(int k, long long i, long long count) {
+  return k < 4 ? 4 * i + k : (k < 8 ? 4 * count + 4 * i + (k - 4) : 8 * count + 2 * i + (k - 8));
+}
+
+// Reduced-precision copy of the medium for the fast kernel (the mixed
+// form): per point 16 bytes (cxx, cyy, cxy, czz, cxz, cyz, v2px, v2pz) then,
+// in a second array, 4 bytes (v2sz, v2pn), as FP16 or BF16.  The four
+// velocity terms are stored scaled by 2^-vexp so they stay in FP16's range;
+// the kernel folds 2^vexp into dt^2.
+enum CoefForm { CF_F32 = 0, CF_VV = 1, CF_F16 = 2, CF_BF16 = 3 };
 // Device slot of each dc_precomp_vars field (reference order ch1dxx, ch1dyy,
 // ch1dzz, ch1dxy, ch1dyz, ch1dxz, v2px, v2pz, v2sz, v2pn).
 constexpr int kRefToDev[10] = {DC_CXX, DC_CYY, DC_CZZ, DC_CXY, DC_CYZ,
@@ -58,8 +72,8 @@ struct StepParams {
   // (pp, qp) and is updated in place, `cur` holds (pc, qc).
   float2 *prev;
   const float2 *cur;
-  const float *coef;            // [DC_NCOEF][count]
-  const float *vv;              // [2][count]: vpz, vsv (VPZ_VSV medium)
+  const float *coef;            // grouped FP32 coefficients (see coef_index)
+  const float *vv;              // (vpz, vsv) pairs (VPZ_VSV medium)
   long long count;              // floats per array (incl. pitch padding)
   const float *sponge;          // gx[sx] | gy[sy] | gz[sz], or null
   int sponge_oy, sponge_oz;     // offsets of gy / gz in `sponge`
@@ -95,8 +109,13 @@ struct Sim {
   // two pair buffers of `count` (p, q) elements; which one is "previous"
   // and which "current" is read from the reference-ABI view (abi.pp/abi.pc)
   float2 *pq[2] = {nullptr, nullptr};
-  float *coef = nullptr;       // [DC_NCOEF][count]
-  float *vv = nullptr;         // [2][count]
+  float *coef = nullptr;       // grouped FP32 coefficients (see coef_index)
+  float *vv = nullptr;         // (vpz, vsv) pairs
+  // reduced-precision copy used by the fast kernel (DC_GB300_MEDIUM_*_F16/BF16)
+  void *coef16 = nullptr;      // [count] x 16 B then [count] x 4 B
+  int coef_form = CF_F32;      // CoefForm the fast kernel reads
+  int vexp = 0;                // velocity terms stored scaled by 2^-vexp
+  bool coef16_stale = true;
   float *sponge = nullptr;     // [sx + sy + sz]
   bool has_sponge = false;
   // source
@@ -122,7 +141,7 @@ struct Sim {
   long long launches = 0;
   int config_version = 0;
   // tensor maps for the fast kernel (encoded for one tile shape)
-  CUtensorMap tm_halo[2], tm_own[2], tm_ca, tm_cb;
+  CUtensorMap tm_halo[2], tm_own[2], tm_c[3];
   int maps_tx = 0, maps_ty = 0;
   // captured multi-step graphs, keyed by start parity of the pc buffer
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -161,11 +180,30 @@ cudaError_t launch_box_copy(cudaStream_t st, float2 *pairs, int comp,
                             const long long b1[3], long long pitch,
                             long long plane, bool to_dense);
 cudaError_t launch_advance_step(cudaStream_t st, int *d_step, int by);
+// Precompute from dense anisotropy arrays (n points) into grouped
+// coefficients at dense indices (count = n); callers repack to the pitch.
 cudaError_t launch_precomp(cudaStream_t st, const float *theta,
                            const float *phi, const float *vsv,
                            const float *vpz, const float *eps,
                            const float *delta, float *coef, long long count,
                            long long n);
+// One coefficient (DevCoef k): dense device array <-> grouped pitched
+// coefficients (count = padded points; pitch = sx and count = n address a
+// dense grouped block).
+cudaError_t launch_coef_component(cudaStream_t st, float *coef, float *dense, int k,
+                                  long long sx, long long sy, long long sz, long long pitch,
+                                  long long count, bool to_grouped);
+// max |v2px|, |v2pz|, |v2sz|, |v2pn| as float bits, atomically into *out.
+cudaError_t launch_coef_vmax(cudaStream_t st, const float *coef, long long count,
+                             unsigned int *out);
+// Grouped dense (count_d = n) -> grouped pitched.
+cudaError_t launch_coef_repitch(cudaStream_t st, float *coef, const float *grouped_dense,
+                                long long sx, long long sy, long long sz, long long pitch,
+                                long long count);
+// FP32 grouped -> FP16/BF16 copy (form CF_F16 or CF_BF16) with velocity
+// terms scaled by 2^-vexp.
+cudaError_t launch_coef_narrow(cudaStream_t st, const float *coef, void *coef16, int form,
+                               int vexp, long long count);
 cudaError_t launch_layered(cudaStream_t st, const dc_gb300_layered_spec &spec,
                            float *coef, float *vv, long long sx, long long sy,
                            long long sz, long long pitch, long long count);
@@ -182,7 +220,7 @@ cudaError_t launch_reference_medium(cudaStream_t st, const int n[3], int absorb,
 bool encode_tiled(CUtensorMap *map, const void *base, int rank,
                   const uint64_t *dims, const uint64_t *strides_bytes,
                   const uint32_t *box, std::string *err,
-                  bool pairs = false);
+                  CUtensorMapDataType type = CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
 
 // Thread-local error text for dc_gb300_last_error().
 void set_error(const std::string &msg);

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -87,20 +88,23 @@ bool roles(const Sim *s, int *cur, int *prev) {
 // Keeps the reference-ABI view in step with the device arrays.
 void refresh_abi(Sim *s) {
   dc_device_data &a = s->handle->abi;
+  // (vpz, vsv) pairs; each coefficient points at its lane of the grouped
+  // layout (see coef_index)
   a.vpz = s->vv;
-  a.vsv = s->vv ? s->vv + s->count : nullptr;
+  a.vsv = s->vv ? s->vv + 1 : nullptr;
   dc_precomp_vars &p = a.precomp_vars;
   float *c = s->coef;
-  p.ch1dxx = c ? c + DC_CXX * s->count : nullptr;
-  p.ch1dyy = c ? c + DC_CYY * s->count : nullptr;
-  p.ch1dzz = c ? c + DC_CZZ * s->count : nullptr;
-  p.ch1dxy = c ? c + DC_CXY * s->count : nullptr;
-  p.ch1dyz = c ? c + DC_CYZ * s->count : nullptr;
-  p.ch1dxz = c ? c + DC_CXZ * s->count : nullptr;
-  p.v2px = c ? c + DC_V2PX * s->count : nullptr;
-  p.v2pz = c ? c + DC_V2PZ * s->count : nullptr;
-  p.v2sz = c ? c + DC_V2SZ * s->count : nullptr;
-  p.v2pn = c ? c + DC_V2PN * s->count : nullptr;
+  const long long n = s->count;
+  p.ch1dxx = c ? c + coef_index(DC_CXX, 0, n) : nullptr;
+  p.ch1dyy = c ? c + coef_index(DC_CYY, 0, n) : nullptr;
+  p.ch1dzz = c ? c + coef_index(DC_CZZ, 0, n) : nullptr;
+  p.ch1dxy = c ? c + coef_index(DC_CXY, 0, n) : nullptr;
+  p.ch1dyz = c ? c + coef_index(DC_CYZ, 0, n) : nullptr;
+  p.ch1dxz = c ? c + coef_index(DC_CXZ, 0, n) : nullptr;
+  p.v2px = c ? c + coef_index(DC_V2PX, 0, n) : nullptr;
+  p.v2pz = c ? c + coef_index(DC_V2PZ, 0, n) : nullptr;
+  p.v2sz = c ? c + coef_index(DC_V2SZ, 0, n) : nullptr;
+  p.v2pn = c ? c + coef_index(DC_V2PN, 0, n) : nullptr;
 }
 
 void drop_graphs(Sim *s) {
@@ -120,6 +124,7 @@ void release(Sim *s) {
     f = nullptr;
   }
   cudaFree(s->coef);
+  cudaFree(s->coef16);
   cudaFree(s->vv);
   cudaFree(s->sponge);
   cudaFree(s->d_src);
@@ -173,6 +178,8 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
   }
   p.dt = dt;
   p.dt2 = dt * dt;
+  // the FP16/BF16 medium stores the velocity terms scaled by 2^-vexp
+  if (s->coef_form == CF_F16 || s->coef_form == CF_BF16) p.dt2 = ldexpf(p.dt2, s->vexp);
   const dc_device_data &a = s->handle->abi;
   p.prev = reinterpret_cast<float2 *>(a.pp);
   p.cur = reinterpret_cast<const float2 *>(a.pc);
@@ -309,7 +316,7 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
     return fail(DC_GB300_ERR_ARG, "size too large");
   if (cfg->kernel != DC_GB300_KERNEL_FAST && cfg->kernel != DC_GB300_KERNEL_EXACT)
     return fail(DC_GB300_ERR_ARG, "unknown kernel");
-  if (cfg->medium != DC_GB300_MEDIUM_PRECOMP && cfg->medium != DC_GB300_MEDIUM_VPZ_VSV)
+  if (cfg->medium < DC_GB300_MEDIUM_PRECOMP || cfg->medium > DC_GB300_MEDIUM_PRECOMP_BF16)
     return fail(DC_GB300_ERR_ARG, "unknown medium form");
   if (!(cfg->dx > 0 && cfg->dy > 0 && cfg->dz > 0 && cfg->dt > 0))
     return fail(DC_GB300_ERR_ARG, "dx, dy, dz and dt must be positive");
@@ -342,7 +349,13 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
   s->dz = cfg->dz;
   s->dt = cfg->dt;
   s->kernel = cfg->kernel;
-  s->medium = cfg->medium;
+  // the narrow forms are the ten-coefficient medium with an FP16/BF16 copy
+  s->medium = cfg->medium == DC_GB300_MEDIUM_VPZ_VSV ? DC_GB300_MEDIUM_VPZ_VSV
+                                                     : DC_GB300_MEDIUM_PRECOMP;
+  s->coef_form = cfg->medium == DC_GB300_MEDIUM_VPZ_VSV       ? CF_VV
+                 : cfg->medium == DC_GB300_MEDIUM_PRECOMP_F16  ? CF_F16
+                 : cfg->medium == DC_GB300_MEDIUM_PRECOMP_BF16 ? CF_BF16
+                                                               : CF_F32;
   auto bail = [&](int code) {
     release(s);
     delete s;
@@ -360,6 +373,9 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
   if (s->medium == DC_GB300_MEDIUM_PRECOMP) {
     if (cudaMalloc(&s->coef, bytes * DC_NCOEF) != cudaSuccess)
       return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of the coefficients failed"));
+    if ((s->coef_form == CF_F16 || s->coef_form == CF_BF16) &&
+        cudaMalloc(&s->coef16, static_cast<size_t>(s->count) * 20) != cudaSuccess)
+      return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of the FP16 coefficients failed"));
   } else {
     if (cudaMalloc(&s->vv, bytes * 2) != cudaSuccess)
       return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of vpz/vsv failed"));
@@ -372,6 +388,7 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
     if (cudaMemsetAsync(s->pq[b], 0, bytes * 2, s->stream) != cudaSuccess)
       return bail(fail(DC_GB300_ERR_CUDA, "cudaMemset failed"));
   if (s->coef) cudaMemsetAsync(s->coef, 0, bytes * DC_NCOEF, s->stream);
+  if (s->coef16) cudaMemsetAsync(s->coef16, 0, static_cast<size_t>(s->count) * 20, s->stream);
   if (s->vv) cudaMemsetAsync(s->vv, 0, bytes * 2, s->stream);
   cudaMemsetAsync(s->d_step, 0, sizeof(int), s->stream);
   cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
@@ -427,6 +444,10 @@ extern "C" long dc_gb300_steps_done(const dc_gb300_sim *h) {
   return h && h->impl ? static_cast<long>(h->impl->steps_done) : 0;
 }
 
+// dc_precomp_vars order -> DevCoef
+constexpr int kRefOrder[10] = {DC_CXX, DC_CYY, DC_CZZ, DC_CXY, DC_CYZ,
+                               DC_CXZ, DC_V2PX, DC_V2PZ, DC_V2SZ, DC_V2PN};
+
 extern "C" int dc_gb300_set_precomp(dc_gb300_sim *h, const dc_precomp_vars *host) {
   Sim *s = impl(h);
   if (!s || !host) return fail(DC_GB300_ERR_ARG, "null argument");
@@ -434,12 +455,20 @@ extern "C" int dc_gb300_set_precomp(dc_gb300_sim *h, const dc_precomp_vars *host
   const float *src[10] = {host->ch1dxx, host->ch1dyy, host->ch1dzz, host->ch1dxy,
                           host->ch1dyz, host->ch1dxz, host->v2px,   host->v2pz,
                           host->v2sz,   host->v2pn};
+  for (const float *p : src)
+    if (!p) return fail(DC_GB300_ERR_ARG, "a coefficient array is null");
   DCG_TRY(cudaSetDevice(s->device));
+  const long long n = s->sx * s->sy * s->sz;
+  float *stage = nullptr;
+  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n, s->stream));
   for (int k = 0; k < 10; ++k) {
-    if (!src[k]) return fail(DC_GB300_ERR_ARG, "a coefficient array is null");
-    DCG_TRY(upload_dense(s, s->coef + kRefToDev[k] * s->count, src[k]));
+    DCG_TRY(cudaMemcpyAsync(stage, src[k], sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+    DCG_TRY(launch_coef_component(s->stream, s->coef, stage, kRefOrder[k], s->sx, s->sy, s->sz,
+                                  s->pitch, s->count, true));
   }
+  DCG_TRY(cudaFreeAsync(stage, s->stream));
   DCG_TRY(cudaStreamSynchronize(s->stream));
+  s->coef16_stale = true;
   return DC_GB300_OK;
 }
 
@@ -448,8 +477,14 @@ extern "C" int dc_gb300_set_vpz_vsv(dc_gb300_sim *h, const float *vpz, const flo
   if (!s || !vpz || !vsv) return fail(DC_GB300_ERR_ARG, "null argument");
   if (!s->vv) return fail(DC_GB300_ERR_STATE, "simulation uses the ten-coefficient medium form");
   DCG_TRY(cudaSetDevice(s->device));
-  DCG_TRY(upload_dense(s, s->vv, vpz));
-  DCG_TRY(upload_dense(s, s->vv + s->count, vsv));
+  const long long n = s->sx * s->sy * s->sz;
+  float *stage = nullptr;
+  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
+  DCG_TRY(cudaMemcpyAsync(stage, vpz, sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+  DCG_TRY(cudaMemcpyAsync(stage + n, vsv, sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+  DCG_TRY(launch_pack(s->stream, reinterpret_cast<float2 *>(s->vv), stage, stage + n, s->sx,
+                      s->sy, s->sz, s->pitch));
+  DCG_TRY(cudaFreeAsync(stage, s->stream));
   DCG_TRY(cudaStreamSynchronize(s->stream));
   return DC_GB300_OK;
 }
@@ -461,8 +496,16 @@ extern "C" int dc_gb300_get_precomp(dc_gb300_sim *h, const dc_precomp_vars *host
   float *dst[10] = {host->ch1dxx, host->ch1dyy, host->ch1dzz, host->ch1dxy, host->ch1dyz,
                     host->ch1dxz, host->v2px,   host->v2pz,   host->v2sz,   host->v2pn};
   DCG_TRY(cudaSetDevice(s->device));
-  for (int k = 0; k < 10; ++k)
-    if (dst[k]) DCG_TRY(download_dense(s, dst[k], s->coef + kRefToDev[k] * s->count));
+  const long long n = s->sx * s->sy * s->sz;
+  float *stage = nullptr;
+  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n, s->stream));
+  for (int k = 0; k < 10; ++k) {
+    if (!dst[k]) continue;
+    DCG_TRY(launch_coef_component(s->stream, s->coef, stage, kRefOrder[k], s->sx, s->sy, s->sz,
+                                  s->pitch, s->count, false));
+    DCG_TRY(cudaMemcpyAsync(dst[k], stage, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream));
+  }
+  DCG_TRY(cudaFreeAsync(stage, s->stream));
   DCG_TRY(cudaStreamSynchronize(s->stream));
   return DC_GB300_OK;
 }
@@ -472,17 +515,23 @@ extern "C" int dc_gb300_get_vpz_vsv(dc_gb300_sim *h, float *vpz, float *vsv) {
   if (!s) return fail(DC_GB300_ERR_ARG, "null argument");
   if (!s->vv) return fail(DC_GB300_ERR_STATE, "simulation uses the ten-coefficient medium form");
   DCG_TRY(cudaSetDevice(s->device));
-  if (vpz) DCG_TRY(download_dense(s, vpz, s->vv));
-  if (vsv) DCG_TRY(download_dense(s, vsv, s->vv + s->count));
+  const long long n = s->sx * s->sy * s->sz;
+  float *stage = nullptr;
+  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
+  DCG_TRY(launch_unpack(s->stream, reinterpret_cast<const float2 *>(s->vv), stage, stage + n,
+                        s->sx, s->sy, s->sz, s->pitch));
+  if (vpz) DCG_TRY(cudaMemcpyAsync(vpz, stage, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream));
+  if (vsv)
+    DCG_TRY(cudaMemcpyAsync(vsv, stage + n, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream));
+  DCG_TRY(cudaFreeAsync(stage, s->stream));
   DCG_TRY(cudaStreamSynchronize(s->stream));
   return DC_GB300_OK;
 }
 
 namespace {
-// GPU FP64 precompute from dense host anisotropy arrays into `coef_dense`
-// (10 dense arrays of n floats, device order).
-int precompute_dense(cudaStream_t st, const dc_anisotropy_t *a, long long n,
-                     float *coef_dense) {
+// GPU FP64 precompute from dense host anisotropy arrays into `grouped`, a
+// dense grouped coefficient block of n points (coef_index with count = n).
+int precompute_dense(cudaStream_t st, const dc_anisotropy_t *a, long long n, float *grouped) {
   const float *src[6] = {a->theta, a->phi, a->vsv, a->vpz, a->epsilon, a->delta};
   for (const float *p : src)
     if (!p) return fail(DC_GB300_ERR_ARG, "an anisotropy array is null");
@@ -492,8 +541,37 @@ int precompute_dense(cudaStream_t st, const dc_anisotropy_t *a, long long n,
     DCG_TRY(cudaMemcpyAsync(d_in + k * n, src[k], sizeof(float) * n,
                             cudaMemcpyHostToDevice, st));
   DCG_TRY(launch_precomp(st, d_in, d_in + n, d_in + 2 * n, d_in + 3 * n, d_in + 4 * n,
-                         d_in + 5 * n, coef_dense, n, n));
+                         d_in + 5 * n, grouped, n, n));
   DCG_TRY(cudaFreeAsync(d_in, st));
+  return DC_GB300_OK;
+}
+
+// Refreshes the FP16/BF16 copy of the medium when the fast kernel reads it:
+// the velocity terms are scaled by 2^-vexp so their maximum stays below 2^14.
+int refresh_narrow(Sim *s) {
+  if (!(s->coef_form == CF_F16 || s->coef_form == CF_BF16) || !s->coef16_stale)
+    return DC_GB300_OK;
+  unsigned int *d_max = nullptr;
+  unsigned int bits = 0;
+  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&d_max), sizeof(unsigned int), s->stream));
+  DCG_TRY(cudaMemsetAsync(d_max, 0, sizeof(unsigned int), s->stream));
+  DCG_TRY(launch_coef_vmax(s->stream, s->coef, s->count, d_max));
+  DCG_TRY(cudaMemcpyAsync(&bits, d_max, sizeof(bits), cudaMemcpyDeviceToHost, s->stream));
+  DCG_TRY(cudaFreeAsync(d_max, s->stream));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  float vmax;
+  std::memcpy(&vmax, &bits, sizeof(vmax));
+  int e = 0;
+  if (vmax > 0.0f && std::isfinite(vmax)) {
+    std::frexp(vmax, &e);  // vmax < 2^e
+    e -= 14;
+  }
+  s->vexp = e;
+  DCG_TRY(launch_coef_narrow(s->stream, s->coef, s->coef16, s->coef_form, s->vexp, s->count));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  s->coef16_stale = false;
+  drop_graphs(s);  // dt^2 in the captured parameters depends on vexp
+  ++s->config_version;
   return DC_GB300_OK;
 }
 }  // namespace
@@ -505,20 +583,19 @@ extern "C" int dc_gb300_set_anisotropy(dc_gb300_sim *h, const dc_anisotropy_t *h
   const long long n = s->sx * s->sy * s->sz;
   if (s->vv) {
     if (!host->vpz || !host->vsv) return fail(DC_GB300_ERR_ARG, "vpz/vsv null");
-    DCG_TRY(upload_dense(s, s->vv, host->vpz));
-    DCG_TRY(upload_dense(s, s->vv + s->count, host->vsv));
+    int rc = dc_gb300_set_vpz_vsv(h, host->vpz, host->vsv);
+    if (rc != DC_GB300_OK) return rc;
   }
   if (s->coef) {
-    float *dense = nullptr;
-    DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&dense), sizeof(float) * n * DC_NCOEF,
+    float *grouped = nullptr;
+    DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&grouped), sizeof(float) * n * DC_NCOEF,
                             s->stream));
-    int rc = precompute_dense(s->stream, host, n, dense);
+    int rc = precompute_dense(s->stream, host, n, grouped);
     if (rc != DC_GB300_OK) return rc;
-    for (int k = 0; k < DC_NCOEF; ++k)
-      DCG_TRY(cudaMemcpy2DAsync(s->coef + k * s->count, s->pitch * 4, dense + k * n,
-                                s->sx * 4, s->sx * 4, s->sy * s->sz,
-                                cudaMemcpyDeviceToDevice, s->stream));
-    DCG_TRY(cudaFreeAsync(dense, s->stream));
+    DCG_TRY(launch_coef_repitch(s->stream, s->coef, grouped, s->sx, s->sy, s->sz, s->pitch,
+                                s->count));
+    DCG_TRY(cudaFreeAsync(grouped, s->stream));
+    s->coef16_stale = true;
   }
   DCG_TRY(cudaStreamSynchronize(s->stream));
   return DC_GB300_OK;
@@ -537,6 +614,7 @@ extern "C" int dc_gb300_generate_layered(dc_gb300_sim *h, const dc_gb300_layered
   DCG_TRY(launch_layered(s->stream, *spec, s->coef, s->vv, s->sx, s->sy, s->sz, s->pitch,
                          s->count));
   DCG_TRY(cudaStreamSynchronize(s->stream));
+  s->coef16_stale = true;
   return DC_GB300_OK;
 }
 
@@ -557,6 +635,7 @@ extern "C" int dc_gb300_generate_reference(dc_gb300_sim *h, long nx, long ny, lo
   DCG_TRY(launch_reference_medium(s->stream, n, static_cast<int>(absorb), seed, consts, s->coef,
                                   s->vv, s->pitch, s->count));
   DCG_TRY(cudaStreamSynchronize(s->stream));
+  s->coef16_stale = true;
   return DC_GB300_OK;
 }
 
@@ -954,6 +1033,10 @@ extern "C" int dc_gb300_run(dc_gb300_sim *h, int steps) {
   DCG_TRY(cudaSetDevice(s->device));
   int cur0 = -1, prev0 = -1;
   if (!roles(s, &cur0, &prev0)) return fail(DC_GB300_ERR_STATE, "field pointers rearranged");
+  if (s->kernel == DC_GB300_KERNEL_FAST) {
+    const int rc = refresh_narrow(s);
+    if (rc != DC_GB300_OK) return rc;
+  }
   if (s->energy_cap > 0 && s->steps_done + steps > s->energy_cap)
     return fail(DC_GB300_ERR_ARG, "run exceeds the energy capacity");
   if (s->nrec > 0 && s->steps_done + steps > s->trace_cap)
@@ -1020,6 +1103,10 @@ extern "C" int dc_gb300_propagate_box(dc_gb300_sim *h, const size_t start[3],
   if (!roles(s, &cur, &prev))
     return fail(DC_GB300_ERR_STATE, "field pointers do not belong to this simulation");
   DCG_TRY(cudaSetDevice(s->device));
+  if (s->kernel == DC_GB300_KERNEL_FAST) {
+    const int rc = refresh_narrow(s);
+    if (rc != DC_GB300_OK) return rc;
+  }
   StepParams p = make_params(s, b0, b1, s->dx, s->dy, s->dz, s->dt);
   DCG_TRY(launch_pass(s, p));
   return DC_GB300_OK;
@@ -1044,8 +1131,10 @@ extern "C" dc_device_data *dc_device_data_init(dc_process_t *process) {
   cfg.dz = process->dz;
   cfg.dt = process->dt;
   cfg.kernel = env_is("DC_GB300_KERNEL", "exact") ? DC_GB300_KERNEL_EXACT : DC_GB300_KERNEL_FAST;
-  cfg.medium = env_is("DC_GB300_MEDIUM", "vpz_vsv") ? DC_GB300_MEDIUM_VPZ_VSV
-                                                    : DC_GB300_MEDIUM_PRECOMP;
+  cfg.medium = env_is("DC_GB300_MEDIUM", "vpz_vsv")        ? DC_GB300_MEDIUM_VPZ_VSV
+               : env_is("DC_GB300_MEDIUM", "precomp_f16")  ? DC_GB300_MEDIUM_PRECOMP_F16
+               : env_is("DC_GB300_MEDIUM", "precomp_bf16") ? DC_GB300_MEDIUM_PRECOMP_BF16
+                                                          : DC_GB300_MEDIUM_PRECOMP;
   const char *dev = std::getenv("DC_GB300_DEVICE");
   cfg.device = dev ? std::atoi(dev) : 0;
   // dt etc. may be left 0 by callers that pass them to dc_propagate only
@@ -1056,7 +1145,7 @@ extern "C" dc_device_data *dc_device_data_init(dc_process_t *process) {
   dc_gb300_sim *h = nullptr;
   if (dc_gb300_create(&cfg, &h) != DC_GB300_OK) abi_die("dc_device_data_init");
   int rc = DC_GB300_OK;
-  if (cfg.medium == DC_GB300_MEDIUM_PRECOMP) {
+  if (cfg.medium != DC_GB300_MEDIUM_VPZ_VSV) {
     if (process->precomp_vars.ch1dxx)
       rc = dc_gb300_set_precomp(h, &process->precomp_vars);
     else
@@ -1216,21 +1305,26 @@ extern "C" dc_precomp_vars dc_compute_precomp_vars(int sx, int sy, int sz,
   }
   if (n == 0) return v;
   cudaStream_t st = nullptr;
-  float *dense = nullptr;
+  float *grouped = nullptr, *stage = nullptr;
   if (cudaStreamCreate(&st) != cudaSuccess ||
-      cudaMallocAsync(reinterpret_cast<void **>(&dense), sizeof(float) * n * DC_NCOEF, st) !=
-          cudaSuccess) {
+      cudaMallocAsync(reinterpret_cast<void **>(&grouped), sizeof(float) * n * DC_NCOEF, st) !=
+          cudaSuccess ||
+      cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n, st) != cudaSuccess) {
     set_error("CUDA set-up failed in dc_compute_precomp_vars");
     abi_die("dc_compute_precomp_vars");
   }
-  if (precompute_dense(st, &anisotropy, n, dense) != DC_GB300_OK) abi_die("dc_compute_precomp_vars");
+  if (precompute_dense(st, &anisotropy, n, grouped) != DC_GB300_OK)
+    abi_die("dc_compute_precomp_vars");
   for (int k = 0; k < 10; ++k)
-    if (cudaMemcpyAsync(*dst[k], dense + kRefToDev[k] * n, sizeof(float) * n,
-                        cudaMemcpyDeviceToHost, st) != cudaSuccess) {
+    if (launch_coef_component(st, grouped, stage, kRefOrder[k], sx, sy, sz, sx, n, false) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(*dst[k], stage, sizeof(float) * n, cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess) {
       set_error("copy-back failed in dc_compute_precomp_vars");
       abi_die("dc_compute_precomp_vars");
     }
-  cudaFreeAsync(dense, st);
+  cudaFreeAsync(grouped, st);
+  cudaFreeAsync(stage, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) {
     set_error("dc_compute_precomp_vars kernel failed");
     abi_die("dc_compute_precomp_vars");

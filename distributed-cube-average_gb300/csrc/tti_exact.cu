@@ -123,21 +123,24 @@ __global__ void __launch_bounds__(128)
                         static_cast<long long>(gy) * sY + gx;
     float cxx, cyy, czz, cxy, cyz, cxz, v2px, v2pz, v2sz, v2pn;
     if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) {
-      const float *c = prm.coef;
       const long long n = prm.count;
-      cxx = __ldg(c + DC_CXX * n + i);
-      cyy = __ldg(c + DC_CYY * n + i);
-      czz = __ldg(c + DC_CZZ * n + i);
-      cxy = __ldg(c + DC_CXY * n + i);
-      cyz = __ldg(c + DC_CYZ * n + i);
-      cxz = __ldg(c + DC_CXZ * n + i);
-      v2px = __ldg(c + DC_V2PX * n + i);
-      v2pz = __ldg(c + DC_V2PZ * n + i);
-      v2sz = __ldg(c + DC_V2SZ * n + i);
-      v2pn = __ldg(c + DC_V2PN * n + i);
+      const float4 g0 = __ldg(reinterpret_cast<const float4 *>(prm.coef) + i);
+      const float4 g1 = __ldg(reinterpret_cast<const float4 *>(prm.coef + 4 * n) + i);
+      const float2 g2 = __ldg(reinterpret_cast<const float2 *>(prm.coef + 8 * n) + i);
+      cxx = g0.x;
+      cyy = g0.y;
+      cxy = g0.z;
+      czz = g0.w;
+      cxz = g1.x;
+      cyz = g1.y;
+      v2px = g1.z;
+      v2pz = g1.w;
+      v2sz = g2.x;
+      v2pn = g2.y;
     } else {
       // include/sample_compute.h:9-18 and :51-54
-      const float vp = __ldg(prm.vv + i), vs = __ldg(prm.vv + prm.count + i);
+      const float2 v = __ldg(reinterpret_cast<const float2 *>(prm.vv) + i);
+      const float vp = v.x, vs = v.y;
       cxx = 0.1459632909f;
       cyy = 0.3540367091f;
       czz = 0.5f;

@@ -3,28 +3,40 @@
 // One pass updates p and q (the coupled pseudo-acoustic TTI system of the
 // reference, include/sample_compute.h:105-185) for every point of a box.
 //
-// Work decomposition: a CTA owns a TX x TY column tile in (x, y) and sweeps
+// Work decomposition: a CTA owns a 32 x TY column tile in (x, y) and sweeps
 // a chunk of output planes along z.  For the leading plane k it receives,
-// by TMA into a NSTAGE-deep shared-memory ring:
-//   * the p and q planes k with a 4-cell halo in x and y,
-//   * cxx, cyy, cxy at plane k   (in-plane coefficients),
-//   * the other seven coefficients and pp, qp at the output plane z = k - 4.
-// Each thread owns one (x, y) column and keeps, in registers, a 9-deep queue
-// per field of the centre value, the unscaled first x-derivative and the
-// unscaled first y-derivative.  The cross derivatives are evaluated in their
-// separable form: with the 8th-order first-derivative weights L1..L4, the
-// reference's 64-point derCross (include/derivatives.h:56-91) equals
-// D_a(D_b p) because its weights are L_ab = L_a * L_b.  So
-//   d2p/dxdy  = D_x of the y-derivative plane (shared memory, per plane),
-//   d2p/dxdz  = D_z of the x-derivative queue (registers),
-//   d2p/dydz  = D_z of the y-derivative queue (registers),
-// and the in-plane part of H1/H2 is formed at the leading plane and delayed
-// four planes in registers.  Rounding differs from the reference's direct
-// sums (see the exact kernel for bit-identical results).
+// by TMA into a 3-deep shared-memory ring:
+//   * the (p, q) pairs of plane k with a 4-cell halo in x and y,
+//   * the coefficients and the (pp, qp) tile of the output plane z = k - 4.
+// Each thread owns one (x, y) column and keeps, in registers, 9-deep queues
+// of (p, q) pairs: the centre value, the x-derivative and the y-derivative.
+// The cross derivatives are evaluated in their separable form: with the
+// 8th-order first-derivative weights L1..L4 the reference's 64-point
+// derCross (include/derivatives.h:56-91) has weights L_ab = L_a * L_b, so it
+// equals D_a(D_b p):
+//   d2/dxdy = D_x of a shared-memory plane of the y-derivative,
+//   d2/dxdz = D_z of the x-derivative queue,
+//   d2/dydz = D_z of the y-derivative queue.
+// The in-plane second derivatives and d2/dxdy of plane k wait four planes in
+// a per-thread shared-memory ring until plane k is the output plane.
+// Rounding differs from the reference's direct sums (the exact kernel is
+// bit-identical).
 //
-// Algorithmic (compulsory) DRAM traffic per point-update: read pc, qc, pp,
-// qp and ten coefficients, write pp and qp: 64 bytes (32 bytes for the
-// vpz/vsv medium form).
+// p and q are processed as pairs with packed f32x2 arithmetic (FFMA2,
+// FADD2, FMUL2): one instruction updates both fields.
+//
+// Medium forms (CoefForm): CF_F32 reads the grouped FP32 coefficients
+// (40 B/point); CF_VV reads (vpz, vsv) with the reference CUDA backend's
+// constant angles (8 B/point); CF_F16 / CF_BF16 read a 20 B/point copy in
+// FP16 / BF16 (the mixed-precision form), converted to FP32 on load -- all
+// arithmetic stays FP32.
+//
+// Compulsory DRAM traffic per point-update: read (pc,qc) 8 B, (pp,qp) 8 B and
+// the medium, write (pp,qp) 8 B: 64 B (CF_F32), 32 B (CF_VV), 44 B (CF_F16,
+// CF_BF16).
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include <cstdio>
 #include <cstdlib>
 
@@ -38,34 +50,39 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per TMA wait
 
 constexpr int align128(int b) { return (b + 127) / 128 * 128; }
 
-template <int TX, int TY, int NSTAGE, int MEDIUM>
+template <int CF>
+struct CoefBytes {
+  // bytes per point of each coefficient group (up to three TMA boxes)
+  static constexpr int G0 = CF == CF_F32 ? 16 : CF == CF_VV ? 8 : 16;
+  static constexpr int G1 = CF == CF_F32 ? 16 : CF == CF_VV ? 0 : 4;
+  static constexpr int G2 = CF == CF_F32 ? 8 : 0;
+};
+
+template <int TX, int TY, int CF>
 struct FastLayout {
+  using CB = CoefBytes<CF>;
   static constexpr int HX = TX + 2 * kHalo;
   static constexpr int HY = TY + 2 * kHalo;
   static constexpr int NT = TX * TY;
-  static constexpr int NCA = MEDIUM == DC_GB300_MEDIUM_PRECOMP ? 3 : 0;
-  static constexpr int NCB = MEDIUM == DC_GB300_MEDIUM_PRECOMP ? 7 : 2;
-  // a halo plane of (p, q) pairs, HY rows of HX pairs
-  static constexpr int HALO_BYTES = align128(HX * HY * 8);
-  static constexpr int TILE4 = NT * 4;  // one coefficient tile (128-B multiple)
+  static constexpr int NSTAGE = 3;
+  static constexpr int HALO_BYTES = align128(HX * HY * 8);  // (p, q) pairs
   static constexpr int OFF_H = 0;
-  static constexpr int OFF_CA = HALO_BYTES;
-  static constexpr int OFF_CB = OFF_CA + NCA * TILE4;
-  static constexpr int OFF_OWN = OFF_CB + NCB * TILE4;  // (pp, qp) pairs
+  static constexpr int OFF_C0 = HALO_BYTES;
+  static constexpr int OFF_C1 = OFF_C0 + NT * CB::G0;
+  static constexpr int OFF_C2 = OFF_C1 + NT * CB::G1;
+  static constexpr int OFF_OWN = align128(OFF_C2 + NT * CB::G2);  // (pp, qp) pairs
   static constexpr int STAGE_BYTES = OFF_OWN + NT * 8;
-  static constexpr int DY_BYTES = align128(TY * HX * 8);  // (dy p, dy q) pairs
-  static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;     // 3 buffers
-  // per-thread ring of the delayed in-plane terms (A_p, A_q, B_p, B_q) of
-  // the last 9 planes
-  static constexpr int OFF_AB = OFF_DY + 3 * DY_BYTES;
-  static constexpr int OFF_BAR = OFF_AB + 9 * NT * 16;
+  static constexpr int DY_BYTES = align128(TY * HX * 8);      // y-derivative plane
+  static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;         // 3 buffers
+  static constexpr int NRING = 5;                             // planes k-4 .. k
+  static constexpr int OFF_R4 = OFF_DY + 3 * DY_BYTES;        // (xx, yy) of a plane
+  static constexpr int OFF_R2 = OFF_R4 + NRING * NT * 16;     // xy of a plane
+  static constexpr int OFF_BAR = OFF_R2 + NRING * NT * 8;
   static constexpr int SMEM_BYTES = OFF_BAR + NSTAGE * 8;
   static constexpr uint32_t TX_HALO = HX * HY * 8u;
-  static constexpr uint32_t TX_CA = NCA * NT * 4u;
-  static constexpr uint32_t TX_OUT = NCB * NT * 4u + NT * 8u;
+  static constexpr uint32_t TX_OUT = NT * (CB::G0 + CB::G1 + CB::G2) + NT * 8u;
   static_assert(TX % 32 == 0, "a warp spans one tile row");
   static_assert(8 * TY <= NT, "halo-column work fits the CTA");
-  static_assert(NSTAGE == 3, "stage index u % 3 is a compile-time constant");
 };
 
 // Packed FP32 pair arithmetic (one instruction updates p and q).
@@ -77,8 +94,7 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 
 // Second derivative of a (p, q) pair with pre-scaled weights w[0..4]
-// (K_i / da^2), summed as two independent chains for instruction-level
-// parallelism.
+// (K_i / da^2), summed as two independent chains.
 __device__ __forceinline__ float2 d2(const float *w, float2 c, float2 m1, float2 p1,
                                      float2 m2, float2 p2, float2 m3, float2 p3,
                                      float2 m4, float2 p4) {
@@ -107,15 +123,57 @@ constexpr float kCxy = 0.4546487134f, kCyz = 0.8414709848f;
 constexpr float kCxz = 0.5403023059f;
 constexpr float kV2pxFactor = 1.48f, kV2pnFactor = 1.2f;
 
-template <int TX, int TY, int MEDIUM, bool SPONGE, bool ISO>
+struct Medium {
+  float cxx, cyy, cxy, czz, cxz, cyz, v2px, v2pz, v2sz, v2pn;
+};
+
+__device__ __forceinline__ float2 h2f(uint32_t v, bool bf16) {
+  if (bf16) {  // bfloat16 -> float: the 16 bits are the float's high half
+    return make_float2(__uint_as_float(v << 16), __uint_as_float(v & 0xffff0000u));
+  }
+  __half2 h;
+  *reinterpret_cast<uint32_t *>(&h) = v;
+  return __half22float2(h);
+}
+
+// The ten coefficients of the thread's point from the stage's tiles.
+template <int CF>
+__device__ __forceinline__ Medium load_medium(const unsigned char *c0, const unsigned char *c1,
+                                              const unsigned char *c2, int ot) {
+  Medium m;
+  if (CF == CF_F32) {
+    const float4 g0 = reinterpret_cast<const float4 *>(c0)[ot];
+    const float4 g1 = reinterpret_cast<const float4 *>(c1)[ot];
+    const float2 g2 = reinterpret_cast<const float2 *>(c2)[ot];
+    m = Medium{g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w, g2.x, g2.y};
+  } else if (CF == CF_VV) {
+    // include/sample_compute.h:51-54
+    const float2 v = reinterpret_cast<const float2 *>(c0)[ot];
+    const float v2pz = v.x * v.x;
+    m = Medium{kCxx, kCyy, kCxy, kCzz, kCxz, kCyz, v2pz * kV2pxFactor, v2pz, v.y * v.y,
+               v2pz * kV2pnFactor};
+  } else {
+    const bool bf = CF == CF_BF16;
+    const uint4 h = reinterpret_cast<const uint4 *>(c0)[ot];
+    const uint32_t h1 = reinterpret_cast<const uint32_t *>(c1)[ot];
+    const float2 a = h2f(h.x, bf), b = h2f(h.y, bf), c = h2f(h.z, bf), d = h2f(h.w, bf),
+                 e = h2f(h1, bf);
+    m = Medium{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x, e.y};
+  }
+  return m;
+}
+
+template <int TX, int TY, int CF, bool SPONGE, bool ISO>
 __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     fast_kernel(const __grid_constant__ CUtensorMap tm_cur,
                 const __grid_constant__ CUtensorMap tm_prev,
-                const __grid_constant__ CUtensorMap tm_ca,
-                const __grid_constant__ CUtensorMap tm_cb,
+                const __grid_constant__ CUtensorMap tm_c0,
+                const __grid_constant__ CUtensorMap tm_c1,
+                const __grid_constant__ CUtensorMap tm_c2,
                 const __grid_constant__ StepParams prm) {
-  constexpr int NSTAGE = 3;
-  using Lay = FastLayout<TX, TY, NSTAGE, MEDIUM>;
+  using Lay = FastLayout<TX, TY, CF>;
+  using CB = CoefBytes<CF>;
+  constexpr int NSTAGE = Lay::NSTAGE;
   constexpr int HX = Lay::HX;
   constexpr int NT = Lay::NT;
   // equal spacing on all axes: one set of weights serves x, y and z
@@ -124,7 +182,7 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
   const float *w2z = ISO ? prm.w2x : prm.w2z, *w1z = ISO ? prm.w1x : prm.w1z;
   // No static shared memory in this kernel: the dynamic window starts at
   // the CTA's shared base, so this alignment holds and every access below
-  // is a shared-space access at a compile-time offset.
+  // is a shared-space access.
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + Lay::OFF_BAR);
 
@@ -150,8 +208,9 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     mbar_init_fence();
     prefetch_tensormap(&tm_cur);
     prefetch_tensormap(&tm_prev);
-    prefetch_tensormap(&tm_cb);
-    if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) prefetch_tensormap(&tm_ca);
+    prefetch_tensormap(&tm_c0);
+    if (CB::G1) prefetch_tensormap(&tm_c1);
+    if (CB::G2) prefetch_tensormap(&tm_c2);
   }
   __syncthreads();
 
@@ -160,17 +219,20 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     const int s = j % NSTAGE;
     unsigned char *st = smem + s * Lay::STAGE_BYTES;
     const int k = zb - kHalo + j;
-    const bool want_ca = Lay::NCA > 0 && j >= kHalo && j < n_it - kHalo;
     const bool want_out = j >= 2 * kHalo;
-    const uint32_t bytes = Lay::TX_HALO + (want_ca ? Lay::TX_CA : 0u) +
-                           (want_out ? Lay::TX_OUT : 0u);
-    mbar_arrive_expect_tx(&bars[s], bytes);
+    mbar_arrive_expect_tx(&bars[s], Lay::TX_HALO + (want_out ? Lay::TX_OUT : 0u));
     tma_load_3d(st + Lay::OFF_H, &tm_cur, x0 - kHalo, y0 - kHalo, k, &bars[s]);
-    if (want_ca) tma_load_4d(st + Lay::OFF_CA, &tm_ca, x0, y0, k, 0, &bars[s]);
     if (want_out) {
-      tma_load_4d(st + Lay::OFF_CB, &tm_cb, x0, y0, k - kHalo,
-                  MEDIUM == DC_GB300_MEDIUM_PRECOMP ? 3 : 0, &bars[s]);
-      tma_load_3d(st + Lay::OFF_OWN, &tm_prev, x0, y0, k - kHalo, &bars[s]);
+      const int z = k - kHalo;
+      // 16-byte groups are 4-D boxes (4 x 4-byte lanes innermost)
+      if (CB::G0 == 16)
+        tma_load_4d(st + Lay::OFF_C0, &tm_c0, 0, x0, y0, z, &bars[s]);
+      else
+        tma_load_3d(st + Lay::OFF_C0, &tm_c0, x0, y0, z, &bars[s]);
+      if (CB::G1 == 16) tma_load_4d(st + Lay::OFF_C1, &tm_c1, 0, x0, y0, z, &bars[s]);
+      if (CB::G1 == 4) tma_load_3d(st + Lay::OFF_C1, &tm_c1, x0, y0, z, &bars[s]);
+      if (CB::G2) tma_load_3d(st + Lay::OFF_C2, &tm_c2, x0, y0, z, &bars[s]);
+      tma_load_3d(st + Lay::OFF_OWN, &tm_prev, x0, y0, z, &bars[s]);
     }
   };
 
@@ -178,17 +240,18 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     for (int j = 0; j < NSTAGE - 1 && j < n_it; ++j) issue(j);
 
   // Register queues of (p, q) pairs indexed by plane mod 9 (compile-time
-  // after unrolling): centre value, x- and y-derivative, and the delayed
-  // in-plane parts A (of H1) and B (of the Laplacian).
+  // after unrolling): centre value, x- and y-derivative.
   float2 cq[9], dxq[9], dyq[9];
-  float4 *abr = reinterpret_cast<float4 *>(smem + Lay::OFF_AB);
   float2 e_acc = make_float2(0.f, 0.f);
   int abort_it = -1;
+  float4 *ring4 = reinterpret_cast<float4 *>(smem + Lay::OFF_R4);
+  float2 *ring2 = reinterpret_cast<float2 *>(smem + Lay::OFF_R2);
 
   // inactive threads of edge tiles may sit past the array: no profile read
   const float gxy = (SPONGE && active)
                         ? prm.sponge[gx] * prm.sponge[prm.sponge_oy + gy]
                         : 1.0f;
+  float gzv = SPONGE ? prm.sponge[prm.sponge_oz + zb] : 1.0f;  // next output plane
   const bool src_col = active && gx == prm.src_x && gy == prm.src_y;
   // receivers of this column at or below the first output plane
   int rk = 0, rend = 0, rnext = -1;
@@ -199,6 +262,9 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     while (rk < rend && prm.rec_z[rk] < zb) ++rk;
     rnext = rk < rend ? prm.rec_z[rk] : -1;
   }
+  // next plane where this column records or injects something
+  int ev = (src_col && prm.src_z >= zb) ? min(rnext < 0 ? 1 << 30 : rnext, prm.src_z)
+                                        : (rnext < 0 ? 1 << 30 : rnext);
   const int c0 = (ty + kHalo) * HX + tx + kHalo;  // centre in a halo plane
   const int od = ty * HX + tx + kHalo;            // centre in a dy plane
   const int ot = ty * TX + tx;                    // centre in a tile
@@ -208,7 +274,8 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
                             static_cast<long long>(gy) * prm.pitch + gx);
 
   uint32_t mpar = 0;  // parity of the outer (9-plane) iteration
-  for (int it0 = 0; it0 < n_it; it0 += 9, mpar ^= 1u) {
+  int rbase = 0;      // it0 mod 5 (ring slot of the first plane of the group)
+  for (int it0 = 0; it0 < n_it; it0 += 9, mpar ^= 1u, rbase = rbase >= 1 ? rbase - 1 : 4) {
 #pragma unroll
     for (int u = 0; u < 9; ++u) {
       const int it = it0 + u;
@@ -255,25 +322,15 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
         // The stage read in iteration it-1 is free: refill it.
         if (tid == 0 && it + NSTAGE - 1 < n_it) issue(it + NSTAGE - 1);
 
-        // ---- in-plane part of H1 and of the Laplacian at plane k
+        // ---- in-plane terms of plane k wait in the ring for 4 planes
         if (it >= kHalo && it < n_it - kHalo) {
-          const float2 xy = d1(w1x, dyb[od - 1], dyb[od + 1], dyb[od - 2],
-                               dyb[od + 2], dyb[od - 3], dyb[od + 3], dyb[od - 4],
-                               dyb[od + 4]);
-          float cxx, cyy, cxy;
-          if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) {
-            const float *ca = reinterpret_cast<const float *>(st + Lay::OFF_CA);
-            cxx = ca[ot];
-            cyy = ca[NT + ot];
-            cxy = ca[2 * NT + ot];
-          } else {
-            cxx = kCxx;
-            cyy = kCyy;
-            cxy = kCxy;
-          }
-          const float2 av = fma2(bc(cxy), xy, fma2(bc(cyy), yy, mul2(bc(cxx), xx)));
-          const float2 bv = add2(xx, yy);
-          abr[u * NT + ot] = make_float4(av.x, av.y, bv.x, bv.y);
+          const float2 xy = d1(w1x, dyb[od - 1], dyb[od + 1], dyb[od - 2], dyb[od + 2],
+                               dyb[od - 3], dyb[od + 3], dyb[od - 4], dyb[od + 4]);
+          int rs = rbase + u;  // it mod 5
+          rs = rs >= 5 ? rs - 5 : rs;
+          rs = rs >= 5 ? rs - 5 : rs;
+          ring4[rs * NT + ot] = make_float4(xx.x, xx.y, yy.x, yy.y);
+          ring2[rs * NT + ot] = xy;
         }
 
         // ---- output plane z = k - 4
@@ -282,71 +339,63 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
           const int m4 = (u + 1) % 9, m3 = (u + 2) % 9, m2 = (u + 3) % 9,
                     m1 = (u + 4) % 9, c = (u + 5) % 9, p1 = (u + 6) % 9,
                     p2 = (u + 7) % 9, p3 = (u + 8) % 9, p4 = u;
-          const float4 ab = abr[c * NT + ot];  // A, B of plane z (own column)
+          int rz = rbase + u + 1;  // (it - 4) mod 5
+          rz = rz >= 5 ? rz - 5 : rz;
+          rz = rz >= 5 ? rz - 5 : rz;
+          const float4 xyy = ring4[rz * NT + ot];
+          const float2 xy = ring2[rz * NT + ot];
           const float2 zz = d2(w2z, cq[c], cq[m1], cq[p1], cq[m2], cq[p2], cq[m3],
                                cq[p3], cq[m4], cq[p4]);
           const float2 xz = d1(w1z, dxq[m1], dxq[p1], dxq[m2], dxq[p2],
                                dxq[m3], dxq[p3], dxq[m4], dxq[p4]);
           const float2 yz = d1(w1z, dyq[m1], dyq[p1], dyq[m2], dyq[p2],
                                dyq[m3], dyq[p3], dyq[m4], dyq[p4]);
-          const float *cb = reinterpret_cast<const float *>(st + Lay::OFF_CB);
-          const float2 *own = reinterpret_cast<const float2 *>(st + Lay::OFF_OWN);
-          float czz, cxz, cyz, v2px, v2pz, v2sz, v2pn;
-          if (MEDIUM == DC_GB300_MEDIUM_PRECOMP) {
-            czz = cb[0 * NT + ot];
-            cxz = cb[1 * NT + ot];
-            cyz = cb[2 * NT + ot];
-            v2px = cb[3 * NT + ot];
-            v2pz = cb[4 * NT + ot];
-            v2sz = cb[5 * NT + ot];
-            v2pn = cb[6 * NT + ot];
-          } else {
-            const float vp = cb[ot], vs = cb[NT + ot];
-            czz = kCzz;
-            cxz = kCxz;
-            cyz = kCyz;
-            v2pz = vp * vp;
-            v2sz = vs * vs;
-            v2px = v2pz * kV2pxFactor;
-            v2pn = v2pz * kV2pnFactor;
-          }
-          // (h1p, h1q) and (h2p, h2q)
-          const float2 h1 = fma2(bc(cyz), yz,
-                                 fma2(bc(cxz), xz, fma2(bc(czz), zz, make_float2(ab.x, ab.y))));
-          const float2 h2 = fma2(bc(-1.0f), h1, add2(make_float2(ab.z, ab.w), zz));
-          const float rhsp = fmaf(v2sz, h1.x - h1.y, fmaf(v2pz, h1.y, v2px * h2.x));
-          const float rhsq = fmaf(-v2sz, h2.x - h2.y, fmaf(v2pz, h1.y, v2pn * h2.x));
+          const Medium md = load_medium<CF>(st + Lay::OFF_C0, st + Lay::OFF_C1,
+                                            st + Lay::OFF_C2, ot);
+          const float2 zx = make_float2(xyy.x, xyy.y), zy = make_float2(xyy.z, xyy.w);
+          // H1 = sum c * d2 over the six second derivatives; the Laplacian
+          // (H1 + H2) = xx + yy + zz
+          float2 h1 = mul2(bc(md.cxx), zx);
+          h1 = fma2(bc(md.cyy), zy, h1);
+          h1 = fma2(bc(md.czz), zz, h1);
+          h1 = fma2(bc(md.cxy), xy, h1);
+          h1 = fma2(bc(md.cxz), xz, h1);
+          h1 = fma2(bc(md.cyz), yz, h1);
+          const float2 h2 = fma2(bc(-1.0f), h1, add2(add2(zx, zy), zz));
+          const float rhsp = fmaf(md.v2sz, h1.x - h1.y, fmaf(md.v2pz, h1.y, md.v2px * h2.x));
+          const float rhsq = fmaf(-md.v2sz, h2.x - h2.y, fmaf(md.v2pz, h1.y, md.v2pn * h2.x));
           const float2 rhs = make_float2(rhsp, rhsq);
-          const float2 pv = own[ot];
+          const float2 pv = reinterpret_cast<const float2 *>(st + Lay::OFF_OWN)[ot];
           const float2 cc = add2(cq[c], cq[c]);  // 2 * current
           float2 nv;
           if (SPONGE) {
-            const int z = zb + it - 2 * kHalo;
-            const float g = gxy * prm.sponge[prm.sponge_oz + z];
+            const float g = gxy * gzv;
             nv = mul2(fma2(rhs, bc(prm.dt2), fma2(bc(-g), pv, cc)), bc(g));
           } else {
             nv = fma2(rhs, bc(prm.dt2), fma2(bc(-1.0f), pv, cc));
           }
+          const int z = zb + it - 2 * kHalo;
+          if (SPONGE && z + 1 < ze) gzv = prm.sponge[prm.sponge_oz + z + 1];
           if (active) {
             if (prm.energy) e_acc = fma2(nv, nv, e_acc);
-            const int z = zb + it - 2 * kHalo;
-            if (z == rnext) {
+            if (z == ev) {  // a receiver and/or the source sits at this point
               const int step = *prm.d_step + prm.step_offset;
-              do {
+              while (z == rnext) {
                 if (step >= 0 && step < prm.trace_cap)
                   prm.traces[static_cast<long long>(step) * prm.nrec + prm.rec_r[rk]] = nv.x;
                 ++rk;
-              } while (rk < rend && prm.rec_z[rk] == z);
-              rnext = rk < rend ? prm.rec_z[rk] : -1;
-            }
-            if (src_col && z == prm.src_z) {
-              const int step = *prm.d_step + prm.step_offset;
-              const float sv =
-                  step + 1 < prm.src_count ? prm.src_table[step + 1] : 0.0f;
-              prm.src_pre[0] = nv.x;
-              prm.src_pre[1] = nv.y;
-              nv.x += sv;
-              nv.y += sv;
+                rnext = rk < rend ? prm.rec_z[rk] : -1;
+              }
+              if (src_col && z == prm.src_z) {
+                const float sv =
+                    step + 1 < prm.src_count ? prm.src_table[step + 1] : 0.0f;
+                prm.src_pre[0] = nv.x;
+                prm.src_pre[1] = nv.y;
+                nv.x += sv;
+                nv.y += sv;
+              }
+              const int nr = rnext < 0 ? 1 << 30 : rnext;
+              ev = (src_col && prm.src_z > z) ? min(nr, prm.src_z) : nr;
             }
             *out = nv;
           }
@@ -386,59 +435,74 @@ done:
   }
 }
 
-// Compiled tile shapes: TX = 32 (one warp per tile row) and TY = 8, 12 or
-// 16 rows (256, 384 or 512 threads), a 3-stage TMA ring.
-constexpr int kTX = 32, kStages = 3;
+// Compiled tile shapes: TX = 32 (one warp per tile row) and TY = 8 or 16
+// rows (256 or 512 threads), a 3-stage TMA ring.
+constexpr int kTX = 32;
 
-template <int TY, int MEDIUM, bool SPONGE, bool ISO>
+template <int TY, int CF, bool SPONGE, bool ISO>
 cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int cur_buf, int prev_buf) {
-  using Lay = FastLayout<kTX, TY, kStages, MEDIUM>;
-  auto kern = fast_kernel<kTX, TY, MEDIUM, SPONGE, ISO>;
+  using Lay = FastLayout<kTX, TY, CF>;
+  auto kern = fast_kernel<kTX, TY, CF, SPONGE, ISO>;
   const int nx = prm.x1 - prm.tile_x0, ny = prm.y1 - prm.tile_y0;
   const int nz = prm.z1 - prm.z0;
   dim3 grid((nx + kTX - 1) / kTX, (ny + TY - 1) / TY, (nz + prm.zchunk - 1) / prm.zchunk);
   kern<<<grid, kTX * TY, Lay::SMEM_BYTES, sim->stream>>>(
-      sim->tm_halo[cur_buf], sim->tm_own[prev_buf], sim->tm_ca, sim->tm_cb, prm);
+      sim->tm_halo[cur_buf], sim->tm_own[prev_buf], sim->tm_c[0], sim->tm_c[1], sim->tm_c[2],
+      prm);
   return cudaGetLastError();
 }
 
-template <int TY, int MEDIUM>
+template <int TY, int CF>
 cudaError_t set_smem_attr_all() {
-  using Lay = FastLayout<kTX, TY, kStages, MEDIUM>;
+  using Lay = FastLayout<kTX, TY, CF>;
   cudaError_t e = cudaSuccess;
   const int b = Lay::SMEM_BYTES;
   const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, MEDIUM, false, false>, attr, b);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, MEDIUM, false, true>, attr, b);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, MEDIUM, true, false>, attr, b);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, MEDIUM, true, true>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, false, false>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, false, true>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, true, false>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, true, true>, attr, b);
   return e;
+}
+
+template <int TY, int CF>
+cudaError_t launch_cf(Sim *sim, const StepParams &prm, int cur, int prev) {
+  const bool sp = prm.sponge != nullptr;
+  const bool iso = sim->dx == sim->dy && sim->dy == sim->dz;
+  if (sp)
+    return iso ? launch_fast_t<TY, CF, true, true>(sim, prm, cur, prev)
+               : launch_fast_t<TY, CF, true, false>(sim, prm, cur, prev);
+  return iso ? launch_fast_t<TY, CF, false, true>(sim, prm, cur, prev)
+             : launch_fast_t<TY, CF, false, false>(sim, prm, cur, prev);
 }
 
 template <int TY>
 cudaError_t launch_ty(Sim *sim, const StepParams &prm, int cur, int prev) {
-  const bool sp = prm.sponge != nullptr;
-  const bool iso = sim->dx == sim->dy && sim->dy == sim->dz;
-  constexpr int P = DC_GB300_MEDIUM_PRECOMP, V = DC_GB300_MEDIUM_VPZ_VSV;
-  if (sim->medium == P) {
-    if (sp) return iso ? launch_fast_t<TY, P, true, true>(sim, prm, cur, prev)
-                       : launch_fast_t<TY, P, true, false>(sim, prm, cur, prev);
-    return iso ? launch_fast_t<TY, P, false, true>(sim, prm, cur, prev)
-               : launch_fast_t<TY, P, false, false>(sim, prm, cur, prev);
+  switch (sim->coef_form) {
+    case CF_VV: return launch_cf<TY, CF_VV>(sim, prm, cur, prev);
+    case CF_F16: return launch_cf<TY, CF_F16>(sim, prm, cur, prev);
+    case CF_BF16: return launch_cf<TY, CF_BF16>(sim, prm, cur, prev);
+    default: return launch_cf<TY, CF_F32>(sim, prm, cur, prev);
   }
-  if (sp) return iso ? launch_fast_t<TY, V, true, true>(sim, prm, cur, prev)
-                     : launch_fast_t<TY, V, true, false>(sim, prm, cur, prev);
-  return iso ? launch_fast_t<TY, V, false, true>(sim, prm, cur, prev)
-             : launch_fast_t<TY, V, false, false>(sim, prm, cur, prev);
+}
+
+template <int TY>
+cudaError_t set_attrs(int form) {
+  switch (form) {
+    case CF_VV: return set_smem_attr_all<TY, CF_VV>();
+    case CF_F16: return set_smem_attr_all<TY, CF_F16>();
+    case CF_BF16: return set_smem_attr_all<TY, CF_BF16>();
+    default: return set_smem_attr_all<TY, CF_F32>();
+  }
 }
 
 // 32 x 8 tiles with two CTAs per SM measured fastest on GB300 (616^3 cube:
-// 2.83 ms per step vs 3.09 ms for 32 x 16 and 3.44 ms for 32 x 12);
-// DC_GB300_FAST_TY=12|16 selects the others.
+// 2.83 ms per step vs 3.09 ms for 32 x 16); DC_GB300_FAST_TY=16 selects the
+// other.
 int chosen_ty() {
   const char *e = std::getenv("DC_GB300_FAST_TY");
   const int v = e ? std::atoi(e) : 0;
-  return (v == 12 || v == 16) ? v : 8;
+  return v == 16 ? 16 : 8;
 }
 
 }  // namespace
@@ -461,50 +525,50 @@ bool fast_encode_maps(Sim *sim, std::string *err) {
   // dynamic shared memory above 48 KB must be enabled per kernel and device
   // (done here, before any stream capture)
   const int kTY = chosen_ty();
-  cudaError_t ae;
-  if (kTY == 8)
-    ae = sim->medium == DC_GB300_MEDIUM_PRECOMP ? set_smem_attr_all<8, DC_GB300_MEDIUM_PRECOMP>()
-                                                : set_smem_attr_all<8, DC_GB300_MEDIUM_VPZ_VSV>();
-  else if (kTY == 12)
-    ae = sim->medium == DC_GB300_MEDIUM_PRECOMP ? set_smem_attr_all<12, DC_GB300_MEDIUM_PRECOMP>()
-                                                : set_smem_attr_all<12, DC_GB300_MEDIUM_VPZ_VSV>();
-  else
-    ae = sim->medium == DC_GB300_MEDIUM_PRECOMP ? set_smem_attr_all<16, DC_GB300_MEDIUM_PRECOMP>()
-                                                : set_smem_attr_all<16, DC_GB300_MEDIUM_VPZ_VSV>();
+  cudaError_t ae = kTY == 16 ? set_attrs<16>(sim->coef_form) : set_attrs<8>(sim->coef_form);
   if (ae != cudaSuccess) {
     *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(ae);
     return false;
   }
-  const uint64_t dims3[3] = {static_cast<uint64_t>(sim->sx),
-                             static_cast<uint64_t>(sim->sy),
-                             static_cast<uint64_t>(sim->sz)};
+  const uint64_t X = sim->sx, Y = sim->sy, Z = sim->sz;
+  const uint64_t P = sim->pitch, PL = sim->plane;
+  const uint64_t dims3[3] = {X, Y, Z};
   // (p, q) pair buffers: 8-byte elements
-  const uint64_t str_pq[2] = {static_cast<uint64_t>(sim->pitch) * 8,
-                              static_cast<uint64_t>(sim->plane) * 8};
-  const uint32_t box_halo[3] = {kTX + 8, kTY + 8, 1};
-  const uint32_t box_own[3] = {kTX, kTY, 1};
+  const uint64_t str8[2] = {P * 8, PL * 8};
+  const uint32_t box_halo[3] = {kTX + 8, static_cast<uint32_t>(kTY) + 8, 1};
+  const uint32_t box_tile[3] = {kTX, static_cast<uint32_t>(kTY), 1};
+  const auto U64 = CU_TENSOR_MAP_DATA_TYPE_UINT64, U32 = CU_TENSOR_MAP_DATA_TYPE_UINT32;
+  const auto F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
   for (int b = 0; b < 2; ++b) {
-    if (!encode_tiled(&sim->tm_halo[b], sim->pq[b], 3, dims3, str_pq, box_halo, err, true))
+    if (!encode_tiled(&sim->tm_halo[b], sim->pq[b], 3, dims3, str8, box_halo, err, U64))
       return false;
-    if (!encode_tiled(&sim->tm_own[b], sim->pq[b], 3, dims3, str_pq, box_own, err, true))
+    if (!encode_tiled(&sim->tm_own[b], sim->pq[b], 3, dims3, str8, box_tile, err, U64))
       return false;
   }
-  // coefficient arrays: 4-byte elements
-  const uint64_t str3[2] = {static_cast<uint64_t>(sim->pitch) * 4,
-                            static_cast<uint64_t>(sim->plane) * 4};
-  const uint64_t str4[3] = {str3[0], str3[1],
-                            static_cast<uint64_t>(sim->count) * 4};
-  if (sim->medium == DC_GB300_MEDIUM_PRECOMP) {
-    const uint64_t dims4[4] = {dims3[0], dims3[1], dims3[2], DC_NCOEF};
-    const uint32_t box_a[4] = {kTX, kTY, 1, 3};
-    const uint32_t box_b[4] = {kTX, kTY, 1, 7};
-    if (!encode_tiled(&sim->tm_ca, sim->coef, 4, dims4, str4, box_a, err)) return false;
-    if (!encode_tiled(&sim->tm_cb, sim->coef, 4, dims4, str4, box_b, err)) return false;
-  } else {
-    const uint64_t dims4[4] = {dims3[0], dims3[1], dims3[2], 2};
-    const uint32_t box_b[4] = {kTX, kTY, 1, 2};
-    if (!encode_tiled(&sim->tm_cb, sim->vv, 4, dims4, str4, box_b, err)) return false;
-    sim->tm_ca = sim->tm_cb;  // unused by this medium form
+  // 16-byte coefficient groups: 4 lanes of 4 bytes innermost
+  const uint64_t dims4[4] = {4, X, Y, Z};
+  const uint64_t str16[3] = {16, P * 16, PL * 16};
+  const uint32_t box16[4] = {4, kTX, static_cast<uint32_t>(kTY), 1};
+  const uint64_t str4[2] = {P * 4, PL * 4};
+  const char *c = reinterpret_cast<const char *>(sim->coef);
+  const long long cnt = sim->count;
+  switch (sim->coef_form) {
+    case CF_F32:
+      if (!encode_tiled(&sim->tm_c[0], c, 4, dims4, str16, box16, err, F32)) return false;
+      if (!encode_tiled(&sim->tm_c[1], c + cnt * 16, 4, dims4, str16, box16, err, F32)) return false;
+      if (!encode_tiled(&sim->tm_c[2], c + cnt * 32, 3, dims3, str8, box_tile, err, U64)) return false;
+      break;
+    case CF_VV:
+      if (!encode_tiled(&sim->tm_c[0], sim->vv, 3, dims3, str8, box_tile, err, U64)) return false;
+      sim->tm_c[1] = sim->tm_c[2] = sim->tm_c[0];  // unused
+      break;
+    default: {  // CF_F16, CF_BF16
+      const char *h = static_cast<const char *>(sim->coef16);
+      if (!encode_tiled(&sim->tm_c[0], h, 4, dims4, str16, box16, err, F32)) return false;
+      if (!encode_tiled(&sim->tm_c[1], h + cnt * 16, 3, dims3, str4, box_tile, err, U32))
+        return false;
+      sim->tm_c[2] = sim->tm_c[0];  // unused
+    }
   }
   sim->maps_tx = kTX;
   sim->maps_ty = kTY;
@@ -512,9 +576,8 @@ bool fast_encode_maps(Sim *sim, std::string *err) {
 }
 
 cudaError_t launch_fast(Sim *sim, const StepParams &prm, int cur_buf, int prev_buf) {
-  if (sim->maps_ty == 8) return launch_ty<8>(sim, prm, cur_buf, prev_buf);
-  if (sim->maps_ty == 12) return launch_ty<12>(sim, prm, cur_buf, prev_buf);
-  return launch_ty<16>(sim, prm, cur_buf, prev_buf);
+  if (sim->maps_ty == 16) return launch_ty<16>(sim, prm, cur_buf, prev_buf);
+  return launch_ty<8>(sim, prm, cur_buf, prev_buf);
 }
 
 }  // namespace dcg

@@ -80,7 +80,10 @@ typedef struct {
  *     qc == pc + 1 and consecutive points of one field are 2 floats apart;
  *   - rows are `pitch` points apart, pitch = sx rounded up to a multiple of
  *     4 (dc_gb300_device_pitch());
- *   - vpz/vsv and the ten precomp arrays are plain pitched float arrays.
+ *   - vpz/vsv are interleaved pairs (vsv == vpz + 1); the ten coefficients
+ *     are grouped per point -- (ch1dxx, ch1dyy, ch1dxy, ch1dzz),
+ *     (ch1dxz, ch1dyz, v2px, v2pz), (v2sz, v2pn) -- and each precomp_vars
+ *     pointer addresses its lane of the group.
  * The reference's host code only hands these pointers back to the entry
  * points below (src/worker.c:482-485, :500-501), which understand the
  * layout; dc_device_data_get_results returns dense host arrays. */
@@ -203,9 +206,15 @@ enum {
 
 /* Medium form read by the stencil. */
 enum {
-  DC_GB300_MEDIUM_PRECOMP = 0, /* ten coefficient arrays (64 B/update) */
-  DC_GB300_MEDIUM_VPZ_VSV = 1  /* vpz/vsv + the reference CUDA backend's
-                                  constant angles (32 B/update) */
+  DC_GB300_MEDIUM_PRECOMP = 0,     /* ten FP32 coefficients (64 B/update) */
+  DC_GB300_MEDIUM_VPZ_VSV = 1,     /* vpz/vsv + the reference CUDA backend's
+                                      constant angles (32 B/update) */
+  DC_GB300_MEDIUM_PRECOMP_F16 = 2, /* mixed precision: the fast kernel reads an
+                                      FP16 copy of the ten coefficients, the
+                                      velocity terms scaled by a power of two;
+                                      arithmetic and wavefields stay FP32
+                                      (44 B/update) */
+  DC_GB300_MEDIUM_PRECOMP_BF16 = 3 /* the same with a BF16 copy */
 };
 
 typedef struct dc_gb300_sim dc_gb300_sim;

@@ -1,0 +1,100 @@
+"""The mixed-precision medium forms (DC_GB300_MEDIUM_PRECOMP_F16 / _BF16):
+the fast kernel reads an FP16/BF16 copy of the ten coefficients (velocity
+terms scaled by 2^-vexp), computes in FP32 and keeps FP32 wavefields.
+
+* Against the oracle run on identically rounded coefficients the result must
+  agree to FP32 reordering noise (rel. L2 <= 1e-5): the kernel adds no error
+  beyond the storage rounding.
+* Against the FP64 oracle on the exact coefficients the storage rounding
+  costs, on a 64^3 + 16 layered medium after 300 steps of dt = 0.8 ms:
+  FP16 <= 1.5e-3, BF16 <= 1e-2 (measured on CPU emulation: 7.3e-4 and
+  4.7e-3).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle.oracle import KIND_F32, KIND_F64, Geometry, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def round_f16(a):
+    return np.asarray(a, np.float32).astype(np.float16).astype(np.float32)
+
+
+def round_bf16(a):
+    u = np.asarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def narrowed(coef, fmt):
+    """Coefficients as the fast kernel sees them: ch1d* rounded directly,
+    the velocity terms (dc_precomp_vars indices 6..9) scaled by 2^-vexp with
+    max < 2^14, rounded, scaled back (exact powers of two)."""
+    rnd = round_f16 if fmt == "f16" else round_bf16
+    vmax = max(float(np.abs(c).max()) for c in coef[6:])
+    _, e0 = math.frexp(vmax)
+    vexp = e0 - 14
+    out = [rnd(c) for c in coef[:6]]
+    out += [(rnd(c * np.float32(2.0 ** -vexp)) * np.float32(2.0 ** vexp)).astype(np.float32)
+            for c in coef[6:]]
+    return out
+
+
+@pytest.fixture(scope="module")
+def layered_case(dc, port):
+    from dc_gb300 import medium
+    geom = Geometry((64, 64, 64), 16)
+    spec = medium.layered_spec(7, geom.sizes)
+    aniso = medium.layered_fields(spec, geom.sizes)
+    coef = port.precomp(aniso)
+    steps, dt = 300, 0.8e-3
+    src = port.source_table(dt, steps, 60.0)
+    sponge = [port.sponge_profile(s, 16, 0.35) for s in geom.sizes]
+    s_idx = geom.index(geom.sizes[0] // 2, geom.sizes[1] // 2, 4 + 16 + 20)
+    z64 = [np.zeros(geom.shape, np.float64) for _ in range(4)]
+    f64 = port.run(KIND_F64, geom.sizes, (12.5,) * 3, dt, steps, *z64, coef=coef,
+                   src_index=s_idx, src=src, sponge=sponge)
+    return geom, coef, steps, dt, src, sponge, s_idx, f64
+
+
+@pytest.mark.parametrize("fmt,medium_form,bound", [("f16", 2, 1.5e-3), ("bf16", 3, 1e-2)])
+def test_mixed_precision_medium(dc, port, layered_case, fmt, medium_form, bound):
+    geom, coef, steps, dt, src, sponge, s_idx, f64 = layered_case
+    with dc.Simulation(geom.sizes, (12.5,) * 3, dt, kernel=dc.KERNEL_FAST, medium=medium_form,
+                       device=0) as sim:
+        sim.set_precomp(coef)
+        sim.set_fields()
+        sim.set_source(s_idx, src)
+        sim.set_sponge(*sponge)
+        sim.run(steps)
+        sim.synchronize()
+        out = sim.get_fields()
+    z = [np.zeros(geom.shape, np.float32) for _ in range(4)]
+    emu = port.run(KIND_F32, geom.sizes, (12.5,) * 3, dt, steps, *z, coef=narrowed(coef, fmt),
+                   src_index=s_idx, src=src, sponge=sponge)
+    assert rel_l2(out["pc"], emu.pc) <= 1e-5 and rel_l2(out["qc"], emu.qc) <= 1e-5
+    err = rel_l2(out["pc"], f64.pc)
+    print(f"{fmt}: rel L2 vs FP64 oracle after {steps} steps = {err:.3e}")
+    assert err <= bound
+
+
+def test_mixed_precision_keeps_fp32_for_exact_kernel(dc, port, layered_case):
+    """The exact kernel ignores the narrow copy and stays bit-identical."""
+    geom, coef, steps, dt, src, sponge, s_idx, f64 = layered_case
+    n = 40
+    with dc.Simulation(geom.sizes, (12.5,) * 3, dt, kernel=dc.KERNEL_EXACT,
+                       medium=dc.MEDIUM_PRECOMP_F16, device=0) as sim:
+        sim.set_precomp(coef)
+        sim.set_fields()
+        sim.set_source(s_idx, src)
+        sim.run(n)
+        sim.synchronize()
+        out = sim.get_fields()
+    z = [np.zeros(geom.shape, np.float32) for _ in range(4)]
+    ref = port.run(KIND_F32, geom.sizes, (12.5,) * 3, dt, n, *z, coef=coef, src_index=s_idx,
+                   src=src)
+    assert np.array_equal(out["pc"], ref.pc)
