@@ -347,18 +347,18 @@ __device__ __forceinline__ __nv_bfloat162 to_h2<__nv_bfloat162>(float a, float b
 }
 
 template <typename H2>
-__global__ void coef_narrow_kernel(const float *coef, H2 *h0, H2 *h1, float vscale,
+__global__ void coef_narrow_kernel(const float *coef, H2 *hl, H2 *ho1, H2 *ho2, float vscale,
                                    long long count) {
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
     const float4 g0 = reinterpret_cast<const float4 *>(coef)[i];
     const float4 g1 = reinterpret_cast<const float4 *>(coef + 4 * count)[i];
     const float2 g2 = reinterpret_cast<const float2 *>(coef + 8 * count)[i];
-    h0[4 * i + 0] = to_h2<H2>(g0.x, g0.y);  // cxx, cyy
-    h0[4 * i + 1] = to_h2<H2>(g0.z, g0.w);  // cxy, czz
-    h0[4 * i + 2] = to_h2<H2>(g1.x, g1.y);  // cxz, cyz
-    h0[4 * i + 3] = to_h2<H2>(g1.z * vscale, g1.w * vscale);  // v2px, v2pz
-    h1[i] = to_h2<H2>(g2.x * vscale, g2.y * vscale);          // v2sz, v2pn
+    hl[2 * i + 0] = to_h2<H2>(g0.x, g0.y);                     // cxx, cyy
+    hl[2 * i + 1] = to_h2<H2>(g0.z, g0.w);                     // cxy, czz
+    ho1[2 * i + 0] = to_h2<H2>(g1.x, g1.y);                    // cxz, cyz
+    ho1[2 * i + 1] = to_h2<H2>(g1.z * vscale, g1.w * vscale);  // v2px, v2pz
+    ho2[i] = to_h2<H2>(g2.x * vscale, g2.y * vscale);          // v2sz, v2pn
   }
 }
 
@@ -393,13 +393,16 @@ cudaError_t launch_coef_narrow(cudaStream_t st, const float *coef, void *coef16,
                                int vexp, long long count) {
   const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((count + 255) / 256, 152 * 32)));
   const float vscale = ldexpf(1.0f, -vexp);
+  // layout: [count] x 8 B (cxx, cyy, cxy, czz), [count] x 8 B (cxz, cyz,
+  // v2px, v2pz), [count] x 4 B (v2sz, v2pn)
   if (form == CF_F16) {
-    __half2 *h0 = static_cast<__half2 *>(coef16);
-    coef_narrow_kernel<__half2><<<blocks, 256, 0, st>>>(coef, h0, h0 + 4 * count, vscale, count);
+    __half2 *h = static_cast<__half2 *>(coef16);
+    coef_narrow_kernel<__half2><<<blocks, 256, 0, st>>>(coef, h, h + 2 * count, h + 4 * count,
+                                                        vscale, count);
   } else {
-    __nv_bfloat162 *h0 = static_cast<__nv_bfloat162 *>(coef16);
-    coef_narrow_kernel<__nv_bfloat162><<<blocks, 256, 0, st>>>(coef, h0, h0 + 4 * count, vscale,
-                                                               count);
+    __nv_bfloat162 *h = static_cast<__nv_bfloat162 *>(coef16);
+    coef_narrow_kernel<__nv_bfloat162><<<blocks, 256, 0, st>>>(coef, h, h + 2 * count,
+                                                               h + 4 * count, vscale, count);
   }
   return cudaGetLastError();
 }

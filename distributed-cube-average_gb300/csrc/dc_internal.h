@@ -43,8 +43,8 @@ __host__ __device__ __forceinline__ long long coef_index(int k, long long i, lon
 }
 
 // Reduced-precision copy of the medium for the fast kernel (the mixed
-// form): per point 16 bytes (cxx, cyy, cxy, czz, cxz, cyz, v2px, v2pz) then,
-// in a second array, 4 bytes (v2sz, v2pn), as FP16 or BF16.  The four
+// form), FP16 or BF16 in three arrays: 8 bytes (cxx, cyy, cxy, czz), 8 bytes
+// (cxz, cyz, v2px, v2pz) and 4 bytes (v2sz, v2pn) per point.  The four
 // velocity terms are stored scaled by 2^-vexp so they stay in FP16's range;
 // the kernel folds 2^vexp into dt^2.
 enum CoefForm { CF_F32 = 0, CF_VV = 1, CF_F16 = 2, CF_BF16 = 3 };
@@ -112,7 +112,7 @@ struct Sim {
   float *coef = nullptr;       // grouped FP32 coefficients (see coef_index)
   float *vv = nullptr;         // (vpz, vsv) pairs
   // reduced-precision copy used by the fast kernel (DC_GB300_MEDIUM_*_F16/BF16)
-  void *coef16 = nullptr;      // [count] x 16 B then [count] x 4 B
+  void *coef16 = nullptr;      // [count] x 8 B, [count] x 8 B, [count] x 4 B
   int coef_form = CF_F32;      // CoefForm the fast kernel reads
   int vexp = 0;                // velocity terms stored scaled by 2^-vexp
   bool coef16_stale = true;

@@ -52,10 +52,11 @@ constexpr int align128(int b) { return (b + 127) / 128 * 128; }
 
 template <int CF>
 struct CoefBytes {
-  // bytes per point of each coefficient group (up to three TMA boxes)
-  static constexpr int G0 = CF == CF_F32 ? 16 : CF == CF_VV ? 8 : 16;
-  static constexpr int G1 = CF == CF_F32 ? 16 : CF == CF_VV ? 0 : 4;
-  static constexpr int G2 = CF == CF_F32 ? 8 : 0;
+  // bytes per point of each coefficient group: L (cxx, cyy, cxy, czz) is
+  // read at the leading plane, O1 and O2 (the rest) at the output plane
+  static constexpr int L = CF == CF_F32 ? 16 : CF == CF_VV ? 0 : 8;
+  static constexpr int O1 = CF == CF_F32 ? 16 : 8;  // VV: (vpz, vsv)
+  static constexpr int O2 = CF == CF_F32 ? 8 : CF == CF_VV ? 0 : 4;
 };
 
 template <int TX, int TY, int CF>
@@ -67,20 +68,22 @@ struct FastLayout {
   static constexpr int NSTAGE = 3;
   static constexpr int HALO_BYTES = align128(HX * HY * 8);  // (p, q) pairs
   static constexpr int OFF_H = 0;
-  static constexpr int OFF_C0 = HALO_BYTES;
-  static constexpr int OFF_C1 = OFF_C0 + NT * CB::G0;
-  static constexpr int OFF_C2 = OFF_C1 + NT * CB::G1;
-  static constexpr int OFF_OWN = align128(OFF_C2 + NT * CB::G2);  // (pp, qp) pairs
+  static constexpr int OFF_L = HALO_BYTES;
+  static constexpr int OFF_O1 = OFF_L + NT * CB::L;
+  static constexpr int OFF_O2 = OFF_O1 + NT * CB::O1;
+  static constexpr int OFF_OWN = align128(OFF_O2 + NT * CB::O2);  // (pp, qp) pairs
   static constexpr int STAGE_BYTES = OFF_OWN + NT * 8;
   static constexpr int DY_BYTES = align128(TY * HX * 8);      // y-derivative plane
   static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;         // 3 buffers
-  static constexpr int NRING = 5;                             // planes k-4 .. k
-  static constexpr int OFF_R4 = OFF_DY + 3 * DY_BYTES;        // (xx, yy) of a plane
-  static constexpr int OFF_R2 = OFF_R4 + NRING * NT * 16;     // xy of a plane
-  static constexpr int OFF_BAR = OFF_R2 + NRING * NT * 8;
+  // per-thread ring of the delayed in-plane terms of the last 9 planes:
+  // (A_p, A_q, B_p, B_q) and czz
+  static constexpr int OFF_RA = OFF_DY + 3 * DY_BYTES;
+  static constexpr int OFF_RZ = OFF_RA + 9 * NT * 16;
+  static constexpr int OFF_BAR = OFF_RZ + 9 * NT * 4;
   static constexpr int SMEM_BYTES = OFF_BAR + NSTAGE * 8;
   static constexpr uint32_t TX_HALO = HX * HY * 8u;
-  static constexpr uint32_t TX_OUT = NT * (CB::G0 + CB::G1 + CB::G2) + NT * 8u;
+  static constexpr uint32_t TX_LEAD = NT * CB::L;
+  static constexpr uint32_t TX_OUT = NT * (CB::O1 + CB::O2) + NT * 8u;
   static_assert(TX % 32 == 0, "a warp spans one tile row");
   static_assert(8 * TY <= NT, "halo-column work fits the CTA");
 };
@@ -136,40 +139,50 @@ __device__ __forceinline__ float2 h2f(uint32_t v, bool bf16) {
   return __half22float2(h);
 }
 
-// The ten coefficients of the thread's point from the stage's tiles.
+// (cxx, cyy, cxy, czz) of the thread's point at the leading plane.
 template <int CF>
-__device__ __forceinline__ Medium load_medium(const unsigned char *c0, const unsigned char *c1,
-                                              const unsigned char *c2, int ot) {
-  Medium m;
+__device__ __forceinline__ float4 load_lead(const unsigned char *l, int ot) {
+  if (CF == CF_F32) return reinterpret_cast<const float4 *>(l)[ot];
+  if (CF == CF_VV) return make_float4(kCxx, kCyy, kCxy, kCzz);
+  const uint2 h = reinterpret_cast<const uint2 *>(l)[ot];
+  const float2 a = h2f(h.x, CF == CF_BF16), b = h2f(h.y, CF == CF_BF16);
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+
+// (cxz, cyz, v2px, v2pz, v2sz, v2pn) of the thread's point at the output
+// plane.
+struct OutMedium {
+  float cxz, cyz, v2px, v2pz, v2sz, v2pn;
+};
+
+template <int CF>
+__device__ __forceinline__ OutMedium load_out(const unsigned char *o1, const unsigned char *o2,
+                                              int ot) {
   if (CF == CF_F32) {
-    const float4 g0 = reinterpret_cast<const float4 *>(c0)[ot];
-    const float4 g1 = reinterpret_cast<const float4 *>(c1)[ot];
-    const float2 g2 = reinterpret_cast<const float2 *>(c2)[ot];
-    m = Medium{g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w, g2.x, g2.y};
-  } else if (CF == CF_VV) {
-    // include/sample_compute.h:51-54
-    const float2 v = reinterpret_cast<const float2 *>(c0)[ot];
-    const float v2pz = v.x * v.x;
-    m = Medium{kCxx, kCyy, kCxy, kCzz, kCxz, kCyz, v2pz * kV2pxFactor, v2pz, v.y * v.y,
-               v2pz * kV2pnFactor};
-  } else {
-    const bool bf = CF == CF_BF16;
-    const uint4 h = reinterpret_cast<const uint4 *>(c0)[ot];
-    const uint32_t h1 = reinterpret_cast<const uint32_t *>(c1)[ot];
-    const float2 a = h2f(h.x, bf), b = h2f(h.y, bf), c = h2f(h.z, bf), d = h2f(h.w, bf),
-                 e = h2f(h1, bf);
-    m = Medium{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x, e.y};
+    const float4 g1 = reinterpret_cast<const float4 *>(o1)[ot];
+    const float2 g2 = reinterpret_cast<const float2 *>(o2)[ot];
+    return OutMedium{g1.x, g1.y, g1.z, g1.w, g2.x, g2.y};
   }
-  return m;
+  if (CF == CF_VV) {
+    // include/sample_compute.h:51-54
+    const float2 v = reinterpret_cast<const float2 *>(o1)[ot];
+    const float v2pz = v.x * v.x;
+    return OutMedium{kCxz, kCyz, v2pz * kV2pxFactor, v2pz, v.y * v.y, v2pz * kV2pnFactor};
+  }
+  const bool bf = CF == CF_BF16;
+  const uint2 h = reinterpret_cast<const uint2 *>(o1)[ot];
+  const uint32_t h2 = reinterpret_cast<const uint32_t *>(o2)[ot];
+  const float2 a = h2f(h.x, bf), b = h2f(h.y, bf), c = h2f(h2, bf);
+  return OutMedium{a.x, a.y, b.x, b.y, c.x, c.y};
 }
 
 template <int TX, int TY, int CF, bool SPONGE, bool ISO>
 __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     fast_kernel(const __grid_constant__ CUtensorMap tm_cur,
                 const __grid_constant__ CUtensorMap tm_prev,
-                const __grid_constant__ CUtensorMap tm_c0,
-                const __grid_constant__ CUtensorMap tm_c1,
-                const __grid_constant__ CUtensorMap tm_c2,
+                const __grid_constant__ CUtensorMap tm_l,
+                const __grid_constant__ CUtensorMap tm_o1,
+                const __grid_constant__ CUtensorMap tm_o2,
                 const __grid_constant__ StepParams prm) {
   using Lay = FastLayout<TX, TY, CF>;
   using CB = CoefBytes<CF>;
@@ -208,9 +221,9 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     mbar_init_fence();
     prefetch_tensormap(&tm_cur);
     prefetch_tensormap(&tm_prev);
-    prefetch_tensormap(&tm_c0);
-    if (CB::G1) prefetch_tensormap(&tm_c1);
-    if (CB::G2) prefetch_tensormap(&tm_c2);
+    if (CB::L) prefetch_tensormap(&tm_l);
+    prefetch_tensormap(&tm_o1);
+    if (CB::O2) prefetch_tensormap(&tm_o2);
   }
   __syncthreads();
 
@@ -219,19 +232,26 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     const int s = j % NSTAGE;
     unsigned char *st = smem + s * Lay::STAGE_BYTES;
     const int k = zb - kHalo + j;
+    const bool want_lead = CB::L > 0 && j >= kHalo && j < n_it - kHalo;
     const bool want_out = j >= 2 * kHalo;
-    mbar_arrive_expect_tx(&bars[s], Lay::TX_HALO + (want_out ? Lay::TX_OUT : 0u));
+    mbar_arrive_expect_tx(&bars[s], Lay::TX_HALO + (want_lead ? Lay::TX_LEAD : 0u) +
+                                        (want_out ? Lay::TX_OUT : 0u));
     tma_load_3d(st + Lay::OFF_H, &tm_cur, x0 - kHalo, y0 - kHalo, k, &bars[s]);
+    // 16-byte groups are 4-D boxes (4 x 4-byte lanes innermost), 8- and
+    // 4-byte groups 3-D boxes of one element per point
+    if (want_lead) {
+      if (CB::L == 16)
+        tma_load_4d(st + Lay::OFF_L, &tm_l, 0, x0, y0, k, &bars[s]);
+      else
+        tma_load_3d(st + Lay::OFF_L, &tm_l, x0, y0, k, &bars[s]);
+    }
     if (want_out) {
       const int z = k - kHalo;
-      // 16-byte groups are 4-D boxes (4 x 4-byte lanes innermost)
-      if (CB::G0 == 16)
-        tma_load_4d(st + Lay::OFF_C0, &tm_c0, 0, x0, y0, z, &bars[s]);
+      if (CB::O1 == 16)
+        tma_load_4d(st + Lay::OFF_O1, &tm_o1, 0, x0, y0, z, &bars[s]);
       else
-        tma_load_3d(st + Lay::OFF_C0, &tm_c0, x0, y0, z, &bars[s]);
-      if (CB::G1 == 16) tma_load_4d(st + Lay::OFF_C1, &tm_c1, 0, x0, y0, z, &bars[s]);
-      if (CB::G1 == 4) tma_load_3d(st + Lay::OFF_C1, &tm_c1, x0, y0, z, &bars[s]);
-      if (CB::G2) tma_load_3d(st + Lay::OFF_C2, &tm_c2, x0, y0, z, &bars[s]);
+        tma_load_3d(st + Lay::OFF_O1, &tm_o1, x0, y0, z, &bars[s]);
+      if (CB::O2) tma_load_3d(st + Lay::OFF_O2, &tm_o2, x0, y0, z, &bars[s]);
       tma_load_3d(st + Lay::OFF_OWN, &tm_prev, x0, y0, z, &bars[s]);
     }
   };
@@ -244,8 +264,8 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
   float2 cq[9], dxq[9], dyq[9];
   float2 e_acc = make_float2(0.f, 0.f);
   int abort_it = -1;
-  float4 *ring4 = reinterpret_cast<float4 *>(smem + Lay::OFF_R4);
-  float2 *ring2 = reinterpret_cast<float2 *>(smem + Lay::OFF_R2);
+  float4 *ring_ab = reinterpret_cast<float4 *>(smem + Lay::OFF_RA);
+  float *ring_czz = reinterpret_cast<float *>(smem + Lay::OFF_RZ);
 
   // inactive threads of edge tiles may sit past the array: no profile read
   const float gxy = (SPONGE && active)
@@ -274,8 +294,7 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
                             static_cast<long long>(gy) * prm.pitch + gx);
 
   uint32_t mpar = 0;  // parity of the outer (9-plane) iteration
-  int rbase = 0;      // it0 mod 5 (ring slot of the first plane of the group)
-  for (int it0 = 0; it0 < n_it; it0 += 9, mpar ^= 1u, rbase = rbase >= 1 ? rbase - 1 : 4) {
+  for (int it0 = 0; it0 < n_it; it0 += 9, mpar ^= 1u) {
 #pragma unroll
     for (int u = 0; u < 9; ++u) {
       const int it = it0 + u;
@@ -322,15 +341,16 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
         // The stage read in iteration it-1 is free: refill it.
         if (tid == 0 && it + NSTAGE - 1 < n_it) issue(it + NSTAGE - 1);
 
-        // ---- in-plane terms of plane k wait in the ring for 4 planes
+        // ---- in-plane part of H1 (A) and of the Laplacian (B) at plane k;
+        // they wait in ring slot u for 4 planes
         if (it >= kHalo && it < n_it - kHalo) {
           const float2 xy = d1(w1x, dyb[od - 1], dyb[od + 1], dyb[od - 2], dyb[od + 2],
                                dyb[od - 3], dyb[od + 3], dyb[od - 4], dyb[od + 4]);
-          int rs = rbase + u;  // it mod 5
-          rs = rs >= 5 ? rs - 5 : rs;
-          rs = rs >= 5 ? rs - 5 : rs;
-          ring4[rs * NT + ot] = make_float4(xx.x, xx.y, yy.x, yy.y);
-          ring2[rs * NT + ot] = xy;
+          const float4 lc = load_lead<CF>(st + Lay::OFF_L, ot);  // cxx, cyy, cxy, czz
+          const float2 av = fma2(bc(lc.z), xy, fma2(bc(lc.y), yy, mul2(bc(lc.x), xx)));
+          const float2 bv = add2(xx, yy);
+          ring_ab[u * NT + ot] = make_float4(av.x, av.y, bv.x, bv.y);
+          ring_czz[u * NT + ot] = lc.w;
         }
 
         // ---- output plane z = k - 4
@@ -339,29 +359,20 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
           const int m4 = (u + 1) % 9, m3 = (u + 2) % 9, m2 = (u + 3) % 9,
                     m1 = (u + 4) % 9, c = (u + 5) % 9, p1 = (u + 6) % 9,
                     p2 = (u + 7) % 9, p3 = (u + 8) % 9, p4 = u;
-          int rz = rbase + u + 1;  // (it - 4) mod 5
-          rz = rz >= 5 ? rz - 5 : rz;
-          rz = rz >= 5 ? rz - 5 : rz;
-          const float4 xyy = ring4[rz * NT + ot];
-          const float2 xy = ring2[rz * NT + ot];
+          const float4 ab = ring_ab[c * NT + ot];  // A, B of plane z
+          const float czz = ring_czz[c * NT + ot];
           const float2 zz = d2(w2z, cq[c], cq[m1], cq[p1], cq[m2], cq[p2], cq[m3],
                                cq[p3], cq[m4], cq[p4]);
           const float2 xz = d1(w1z, dxq[m1], dxq[p1], dxq[m2], dxq[p2],
                                dxq[m3], dxq[p3], dxq[m4], dxq[p4]);
           const float2 yz = d1(w1z, dyq[m1], dyq[p1], dyq[m2], dyq[p2],
                                dyq[m3], dyq[p3], dyq[m4], dyq[p4]);
-          const Medium md = load_medium<CF>(st + Lay::OFF_C0, st + Lay::OFF_C1,
-                                            st + Lay::OFF_C2, ot);
-          const float2 zx = make_float2(xyy.x, xyy.y), zy = make_float2(xyy.z, xyy.w);
+          const OutMedium md = load_out<CF>(st + Lay::OFF_O1, st + Lay::OFF_O2, ot);
           // H1 = sum c * d2 over the six second derivatives; the Laplacian
           // (H1 + H2) = xx + yy + zz
-          float2 h1 = mul2(bc(md.cxx), zx);
-          h1 = fma2(bc(md.cyy), zy, h1);
-          h1 = fma2(bc(md.czz), zz, h1);
-          h1 = fma2(bc(md.cxy), xy, h1);
-          h1 = fma2(bc(md.cxz), xz, h1);
-          h1 = fma2(bc(md.cyz), yz, h1);
-          const float2 h2 = fma2(bc(-1.0f), h1, add2(add2(zx, zy), zz));
+          const float2 h1 =
+              fma2(bc(md.cyz), yz, fma2(bc(md.cxz), xz, fma2(bc(czz), zz, make_float2(ab.x, ab.y))));
+          const float2 h2 = fma2(bc(-1.0f), h1, add2(make_float2(ab.z, ab.w), zz));
           const float rhsp = fmaf(md.v2sz, h1.x - h1.y, fmaf(md.v2pz, h1.y, md.v2px * h2.x));
           const float rhsq = fmaf(-md.v2sz, h2.x - h2.y, fmaf(md.v2pz, h1.y, md.v2pn * h2.x));
           const float2 rhs = make_float2(rhsp, rhsq);
@@ -448,7 +459,7 @@ cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int cur_buf, int prev
   dim3 grid((nx + kTX - 1) / kTX, (ny + TY - 1) / TY, (nz + prm.zchunk - 1) / prm.zchunk);
   kern<<<grid, kTX * TY, Lay::SMEM_BYTES, sim->stream>>>(
       sim->tm_halo[cur_buf], sim->tm_own[prev_buf], sim->tm_c[0], sim->tm_c[1], sim->tm_c[2],
-      prm);
+      prm);  // tm_c: L, O1, O2
   return cudaGetLastError();
 }
 
@@ -552,6 +563,7 @@ bool fast_encode_maps(Sim *sim, std::string *err) {
   const uint64_t str4[2] = {P * 4, PL * 4};
   const char *c = reinterpret_cast<const char *>(sim->coef);
   const long long cnt = sim->count;
+  // tm_c[0] = L (cxx, cyy, cxy, czz), tm_c[1] = O1, tm_c[2] = O2
   switch (sim->coef_form) {
     case CF_F32:
       if (!encode_tiled(&sim->tm_c[0], c, 4, dims4, str16, box16, err, F32)) return false;
@@ -559,15 +571,15 @@ bool fast_encode_maps(Sim *sim, std::string *err) {
       if (!encode_tiled(&sim->tm_c[2], c + cnt * 32, 3, dims3, str8, box_tile, err, U64)) return false;
       break;
     case CF_VV:
-      if (!encode_tiled(&sim->tm_c[0], sim->vv, 3, dims3, str8, box_tile, err, U64)) return false;
-      sim->tm_c[1] = sim->tm_c[2] = sim->tm_c[0];  // unused
+      if (!encode_tiled(&sim->tm_c[1], sim->vv, 3, dims3, str8, box_tile, err, U64)) return false;
+      sim->tm_c[0] = sim->tm_c[2] = sim->tm_c[1];  // unused
       break;
-    default: {  // CF_F16, CF_BF16
+    default: {  // CF_F16, CF_BF16: 8-byte L, 8-byte O1, 4-byte O2
       const char *h = static_cast<const char *>(sim->coef16);
-      if (!encode_tiled(&sim->tm_c[0], h, 4, dims4, str16, box16, err, F32)) return false;
-      if (!encode_tiled(&sim->tm_c[1], h + cnt * 16, 3, dims3, str4, box_tile, err, U32))
+      if (!encode_tiled(&sim->tm_c[0], h, 3, dims3, str8, box_tile, err, U64)) return false;
+      if (!encode_tiled(&sim->tm_c[1], h + cnt * 8, 3, dims3, str8, box_tile, err, U64)) return false;
+      if (!encode_tiled(&sim->tm_c[2], h + cnt * 16, 3, dims3, str4, box_tile, err, U32))
         return false;
-      sim->tm_c[2] = sim->tm_c[0];  // unused
     }
   }
   sim->maps_tx = kTX;
