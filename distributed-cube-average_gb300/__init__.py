@@ -165,6 +165,8 @@ SIGNATURES = [
     ("dc_gb300_load_checkpoint", C.c_int, [C.c_void_p, C.c_char_p]),
     ("dc_gb300_kernel_launches", C.c_long, [C.c_void_p]),
     ("dc_gb300_stream", C.c_void_p, [C.c_void_p]),
+    ("dc_gb300_exact_steps_noalloc", C.c_int,
+     [C.c_void_p, C.POINTER(C.c_void_p), C.c_void_p, C.c_int, _dp, C.c_void_p]),
     ("dc_gb300_source", C.c_float, [C.c_float, C.c_int, C.c_double]),
     ("dc_gb300_sponge_profile", None, [C.c_long, C.c_long, C.c_double, _fp]),
 ]

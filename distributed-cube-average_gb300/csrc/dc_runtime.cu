@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1331,4 +1332,157 @@ extern "C" dc_precomp_vars dc_compute_precomp_vars(int sx, int sy, int sz,
   }
   cudaStreamDestroy(st);
   return v;
+}
+
+// ---------------------------------------------------------------------------
+// The exact stencil over caller-owned device buffers, with no device
+// allocation at all.
+//
+// Some callers cannot call cudaMalloc: applications that own every byte of
+// device memory themselves (a pre-sized pool, buffers registered once with a
+// communication library) and time loops that must not allocate between
+// steps.  dc_gb300_exact_steps_noalloc serves them: the wavefields and the
+// medium are the caller's device buffers, and the only other memory the
+// kernel needs -- the per-step energy accumulators and the step counter --
+// is the file-scope array below, a fixed 33 KB per device.
+namespace {
+
+// Largest number of steps one call may run: one double energy accumulator
+// per step.
+constexpr int kNoAllocMaxSteps = 4096;
+constexpr size_t kEnergyBytes = sizeof(double) * kNoAllocMaxSteps;
+constexpr size_t kScratchBytes = kEnergyBytes + 256;  // + step counter
+
+// Shared by every call on a device; keeps the last call's contents.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+void *g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array, looked up once per device with that
+// device current.
+int scratch_for(int dev, void **ptr) {
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (!g_scratch_ptr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return dcg::fail(DC_GB300_ERR_CUDA,
+                  std::string("cudaGetSymbolAddress(no-allocation scratch): ") +
+                      cudaGetErrorString(e));
+    g_scratch_ptr[dev] = p;
+  }
+  *ptr = g_scratch_ptr[dev];
+  return DC_GB300_OK;
+}
+
+int run_steps(const dc_gb300_config *cfg, int dev, float *pairs[2], const float *medium,
+              int steps, double *energy, cudaStream_t stream) {
+  void *scratch = nullptr;
+  const int rc = scratch_for(dev, &scratch);
+  if (rc != DC_GB300_OK) return rc;
+  double *e_dev = static_cast<double *>(scratch);
+  int *step_dev = reinterpret_cast<int *>(static_cast<unsigned char *>(scratch) + kEnergyBytes);
+
+#define NOALLOC_TRY(call)                                                     \
+  do {                                                                        \
+    const cudaError_t e_ = (call);                                            \
+    if (e_ != cudaSuccess)                                                    \
+      return dcg::fail(DC_GB300_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+  // the accumulators of this call and the step counter start at zero
+  NOALLOC_TRY(cudaMemsetAsync(e_dev, 0, sizeof(double) * steps, stream));
+  NOALLOC_TRY(cudaMemsetAsync(step_dev, 0, sizeof(int), stream));
+
+  // A host-only description of the caller's buffers, enough for the
+  // library's own parameter set-up and exact-kernel launcher.
+  dc_gb300_sim handle{};
+  dcg::Sim sim;
+  sim.handle = &handle;
+  handle.impl = &sim;
+  sim.device = dev;
+  sim.sx = cfg->sx;
+  sim.sy = cfg->sy;
+  sim.sz = cfg->sz;
+  sim.pitch = (static_cast<long long>(cfg->sx) + 3) / 4 * 4;
+  sim.plane = sim.pitch * cfg->sy;
+  sim.count = sim.plane * cfg->sz;
+  sim.kernel = DC_GB300_KERNEL_EXACT;
+  sim.medium = cfg->medium;
+  sim.stream = stream;
+  if (cfg->medium == DC_GB300_MEDIUM_PRECOMP)
+    sim.coef = const_cast<float *>(medium);
+  else
+    sim.vv = const_cast<float *>(medium);
+  sim.d_step = step_dev;
+
+  const long long b0[3] = {4, 4, 4};
+  const long long b1[3] = {cfg->sx - 4, cfg->sy - 4, cfg->sz - 4};
+  for (int j = 0; j < steps; ++j) {
+    handle.abi.pp = pairs[0];
+    handle.abi.qp = pairs[0] + 1;
+    handle.abi.pc = pairs[1];
+    handle.abi.qc = pairs[1] + 1;
+    dcg::StepParams prm = dcg::make_params(&sim, b0, b1, cfg->dx, cfg->dy, cfg->dz, cfg->dt);
+    prm.energy = energy ? e_dev : nullptr;
+    prm.energy_cap = steps;
+    prm.step_offset = j;
+    NOALLOC_TRY(dcg::launch_exact(&sim, prm));
+    float *t = pairs[0];  // the new field was written over the previous one
+    pairs[0] = pairs[1];
+    pairs[1] = t;
+  }
+  if (energy)
+    NOALLOC_TRY(cudaMemcpyAsync(energy, e_dev, sizeof(double) * steps, cudaMemcpyDeviceToHost,
+                                stream));
+  NOALLOC_TRY(cudaStreamSynchronize(stream));
+#undef NOALLOC_TRY
+  return DC_GB300_OK;
+}
+
+}  // namespace
+
+extern "C" int dc_gb300_exact_steps_noalloc(const dc_gb300_config *cfg, float *pairs[2],
+                                            const float *medium, int steps, double *energy,
+                                            void *stream) {
+  if (!cfg || !pairs || !pairs[0] || !pairs[1] || !medium)
+    return dcg::fail(DC_GB300_ERR_ARG, "null argument");
+  if (steps < 0) return dcg::fail(DC_GB300_ERR_ARG, "negative step count");
+  if (steps > kNoAllocMaxSteps)
+    return dcg::fail(DC_GB300_ERR_ARG,
+                "dc_gb300_exact_steps_noalloc: " + std::to_string(steps) +
+                    " steps exceed the no-allocation scratch maximum of " +
+                    std::to_string(kNoAllocMaxSteps) + " steps per call");
+  if (cfg->sx < 9 || cfg->sy < 9 || cfg->sz < 9)
+    return dcg::fail(DC_GB300_ERR_ARG, "every padded size must be at least 9");
+  if (cfg->sx > (1 << 30) || cfg->sy > (1 << 30) || cfg->sz > (1 << 30))
+    return dcg::fail(DC_GB300_ERR_ARG, "size too large");
+  if (cfg->kernel != DC_GB300_KERNEL_EXACT)
+    return dcg::fail(DC_GB300_ERR_ARG, "dc_gb300_exact_steps_noalloc runs the exact kernel only");
+  if (cfg->medium != DC_GB300_MEDIUM_PRECOMP && cfg->medium != DC_GB300_MEDIUM_VPZ_VSV)
+    return dcg::fail(DC_GB300_ERR_ARG,
+                "dc_gb300_exact_steps_noalloc takes the precomp or vpz/vsv medium form");
+  if (!(cfg->dx > 0 && cfg->dy > 0 && cfg->dz > 0 && cfg->dt > 0))
+    return dcg::fail(DC_GB300_ERR_ARG, "dx, dy, dz and dt must be positive");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return dcg::fail(DC_GB300_ERR_DEVICE, "no CUDA device");
+  int dev = cfg->device;
+  int prev_dev = 0;
+  if (cudaGetDevice(&prev_dev) != cudaSuccess) return dcg::fail(DC_GB300_ERR_CUDA, "cudaGetDevice");
+  if (dev < 0) dev = prev_dev;
+  if (dev >= ndev || dev >= kMaxDevices)
+    return dcg::fail(DC_GB300_ERR_DEVICE, "device ordinal out of range");
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  if (major != 10 || minor != 3)
+    return dcg::fail(DC_GB300_ERR_DEVICE, "this build targets sm_103a");
+  if (cudaSetDevice(dev) != cudaSuccess) return dcg::fail(DC_GB300_ERR_CUDA, "cudaSetDevice");
+  const int rc = run_steps(cfg, dev, pairs, medium, steps, energy,
+                           static_cast<cudaStream_t>(stream));
+  cudaSetDevice(prev_dev);
+  return rc;
 }

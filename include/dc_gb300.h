@@ -358,6 +358,39 @@ float dc_gb300_source(float dt, int it, double fcut);
  * physical interior .. a next to the halo), 1 elsewhere. */
 void dc_gb300_sponge_profile(long s, long a, double kappa, float *g);
 
+/* Runs `steps` time steps of the exact kernel (reference arithmetic, no
+ * source, no sponge) over caller-owned device buffers and allocates no
+ * device memory.  No counterpart in the reference: it serves callers that
+ * cannot call cudaMalloc -- applications that own all device memory
+ * themselves (a pre-sized pool, buffers registered with a communication
+ * library) and time loops that must not allocate between steps.
+ *
+ *   cfg     sizes, spacings, dt, device; kernel must be
+ *           DC_GB300_KERNEL_EXACT, medium DC_GB300_MEDIUM_PRECOMP or
+ *           DC_GB300_MEDIUM_VPZ_VSV
+ *   pairs   {previous, current}: two device buffers of interleaved (p, q)
+ *           pairs, pitch = round_up(sx, 4) points per row, sy*sz rows --
+ *           the layout of dc_device_data; on return pairs[1] holds the
+ *           newest field and pairs[0] the one before it
+ *   medium  device buffer in the grouped coefficient layout (PRECOMP) or
+ *           of (vpz, vsv) pairs (VPZ_VSV), same pitch
+ *   steps   0 .. 4096 (the scratch maximum); larger counts fail with
+ *           DC_GB300_ERR_ARG and an explanatory message
+ *   energy  host array of `steps` doubles receiving the per-step energy
+ *           sum(p^2 + q^2) of each new field, or NULL
+ *   stream  cudaStream_t to run on (NULL = legacy default stream);
+ *           synchronised before return
+ *
+ * The only device memory used besides the caller's buffers is a fixed
+ * 33 KB file-scope scratch array per device (per-step energy accumulators
+ * and a step counter).  The first call on a device looks up its address
+ * (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  Each call clears the part of the scratch it uses; all calls on
+ * a device share it, so calls that overlap on the GPU race. */
+int dc_gb300_exact_steps_noalloc(const dc_gb300_config *cfg, float *pairs[2],
+                                 const float *medium, int steps, double *energy,
+                                 void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,130 @@
+"""dc_gb300_exact_steps_noalloc: the exact stencil over caller-owned device
+buffers, no device allocation.  Checked through the C ABI against the
+simulation entry points (dc_gb300_run with the exact kernel) on two calls in
+a row, within the tolerance of the parity tests (relative L2 <= 1e-5 for the
+fields, relative difference <= 1e-5 for each step's energy).
+
+The file is named so that pytest collects it last; it also passes alone in a
+fresh process, where its first call does the per-device scratch set-up."""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle.oracle import rel_l2
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+TOL = 1e-5
+
+# reference coefficient order (include/precomp.h:6-26) -> grouped lanes
+# (cxx, cyy, cxy, czz | cxz, cyz, v2px, v2pz | v2sz, v2pn)
+_REF_TO_LANE = {0: (0, 0), 1: (0, 1), 2: (0, 3), 3: (0, 2), 4: (1, 1), 5: (1, 0),
+                6: (1, 2), 7: (1, 3), 8: (2, 0), 9: (2, 1)}
+
+
+def _pitched(a, pitch):
+    sz, sy, sx = a.shape
+    out = np.zeros((sz, sy, pitch), a.dtype)
+    out[:, :, :sx] = a
+    return out
+
+
+def _grouped(coef, pitch):
+    sz, sy, _ = coef[0].shape
+    count = sz * sy * pitch
+    g0 = np.zeros((count, 4), np.float32)
+    g1 = np.zeros((count, 4), np.float32)
+    g2 = np.zeros((count, 2), np.float32)
+    groups = (g0, g1, g2)
+    for k, (grp, lane) in _REF_TO_LANE.items():
+        groups[grp][:, lane] = _pitched(coef[k], pitch).reshape(-1)
+    return np.concatenate([g0.reshape(-1), g1.reshape(-1), g2.reshape(-1)])
+
+
+def _pairs(p, q, pitch):
+    return np.stack([_pitched(p, pitch), _pitched(q, pitch)], axis=-1).reshape(-1)
+
+
+def _unpair(buf, shape, pitch):
+    sz, sy, sx = shape
+    a = buf.reshape(sz, sy, pitch, 2)[:, :, :sx, :]
+    return np.ascontiguousarray(a[..., 0]), np.ascontiguousarray(a[..., 1])
+
+
+def _config(dc, sizes, d, dt):
+    return dc.Config(sizes[0], sizes[1], sizes[2], d[0], d[1], d[2], dt, dc.KERNEL_EXACT,
+                     dc.MEDIUM_PRECOMP, 0)
+
+
+def _inputs():
+    g = dict(np.load(GOLDEN / "hetero.npz"))
+    sizes = tuple(int(v) for v in g["sizes"])
+    coef = [g[f"coef{k}"] for k in range(10)]
+    shape = (sizes[2], sizes[1], sizes[0])
+    rng = np.random.default_rng(7)
+    fields = [rng.standard_normal(shape).astype(np.float32) for _ in range(4)]
+    for f in fields:  # the 4-cell halo stays zero, as in the reference
+        f[:4], f[-4:], f[:, :4], f[:, -4:], f[:, :, :4], f[:, :, -4:] = 0, 0, 0, 0, 0, 0
+    return sizes, tuple(float(v) for v in g["d"]), float(g["dt"]), coef, fields
+
+
+def test_noalloc_matches_simulation_on_two_calls(dc):
+    torch = pytest.importorskip("torch")
+    sizes, d, dt, coef, (pp, pc, qp, qc) = _inputs()
+    n = 12
+    # existing entry points: a simulation running 2n steps with energy
+    with dc.Simulation(sizes, d, dt, kernel=dc.KERNEL_EXACT, medium=dc.MEDIUM_PRECOMP,
+                       device=0) as sim:
+        sim.set_precomp(coef)
+        sim.set_fields(pp, pc, qp, qc)
+        sim.enable_energy(2 * n)
+        sim.run(n)
+        sim.synchronize()
+        want = [sim.get_fields()]
+        sim.run(n)
+        sim.synchronize()
+        want.append(sim.get_fields())
+        want_e = sim.energy(2 * n)
+
+    # caller-owned device buffers (allocated here by the test, not by the
+    # entry point)
+    pitch = (sizes[0] + 3) // 4 * 4
+    shape = (sizes[2], sizes[1], sizes[0])
+    dev = torch.device("cuda", 0)
+    prev = torch.from_numpy(_pairs(pp, qp, pitch)).to(dev)
+    cur = torch.from_numpy(_pairs(pc, qc, pitch)).to(dev)
+    medium = torch.from_numpy(_grouped(coef, pitch)).to(dev)
+    torch.cuda.synchronize()
+    by_ptr = {prev.data_ptr(): prev, cur.data_ptr(): cur}
+    cfg = _config(dc, sizes, d, dt)
+    pairs = (C.c_void_p * 2)(prev.data_ptr(), cur.data_ptr())
+    lib = dc.lib()
+    for call in range(2):
+        energy = np.zeros(n, np.float64)
+        rc = lib.dc_gb300_exact_steps_noalloc(
+            C.byref(cfg), pairs, C.c_void_p(medium.data_ptr()), n,
+            energy.ctypes.data_as(C.POINTER(C.c_double)), None)
+        assert rc == 0, lib.dc_gb300_last_error().decode()
+        newest = by_ptr[pairs[1]].cpu().numpy()
+        before = by_ptr[pairs[0]].cpu().numpy()
+        p_new, q_new = _unpair(newest, shape, pitch)
+        p_old, q_old = _unpair(before, shape, pitch)
+        w = want[call]
+        assert rel_l2(p_new, w["pc"]) <= TOL and rel_l2(q_new, w["qc"]) <= TOL
+        assert rel_l2(p_old, w["pp"]) <= TOL and rel_l2(q_old, w["qp"]) <= TOL
+        ref_e = want_e[call * n:(call + 1) * n]
+        assert np.all(ref_e > 0)
+        assert np.max(np.abs(energy - ref_e) / ref_e) <= TOL
+
+
+def test_noalloc_rejects_steps_beyond_scratch(dc):
+    sizes, d, dt, _, _ = _inputs()
+    cfg = _config(dc, sizes, d, dt)
+    dummy = (C.c_void_p * 2)(16, 32)  # never dereferenced: the count is checked first
+    lib = dc.lib()
+    rc = lib.dc_gb300_exact_steps_noalloc(C.byref(cfg), dummy, C.c_void_p(48), 4097, None, None)
+    assert rc == dc.ERR_ARG
+    msg = lib.dc_gb300_last_error().decode()
+    assert "4096" in msg and "maximum" in msg
