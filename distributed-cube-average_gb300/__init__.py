@@ -109,6 +109,19 @@ class LayeredSpec(C.Structure):
     ]
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [("mx", C.c_long), ("my", C.c_long), ("mz", C.c_long),
+                ("dx", C.c_float), ("dy", C.c_float), ("dz", C.c_float), ("dt", C.c_float),
+                ("medium", C.c_int), ("device", C.c_int), ("max_steps", C.c_int)]
+
+
+class Shot(C.Structure):
+    _fields_ = [("sx", C.c_long), ("sy", C.c_long), ("sz", C.c_long),
+                ("ox", C.c_long), ("oy", C.c_long), ("oz", C.c_long),
+                ("src_x", C.c_long), ("src_y", C.c_long), ("src_z", C.c_long),
+                ("fcut", C.c_double), ("absorb", C.c_long), ("kappa", C.c_double)]
+
+
 _sz3 = C.c_size_t * 3
 _i3 = C.c_int * 3
 
@@ -165,6 +178,25 @@ SIGNATURES = [
     ("dc_gb300_load_checkpoint", C.c_int, [C.c_void_p, C.c_char_p]),
     ("dc_gb300_kernel_launches", C.c_long, [C.c_void_p]),
     ("dc_gb300_stream", C.c_void_p, [C.c_void_p]),
+    ("dc_gb300_batch_create", C.c_int, [C.POINTER(BatchConfig), C.POINTER(C.c_void_p)]),
+    ("dc_gb300_batch_destroy", C.c_int, [C.c_void_p]),
+    ("dc_gb300_batch_generate_layered", C.c_int, [C.c_void_p, C.POINTER(LayeredSpec)]),
+    ("dc_gb300_batch_set_precomp", C.c_int, [C.c_void_p, C.POINTER(PrecompVars)]),
+    ("dc_gb300_batch_add_shot", C.c_int, [C.c_void_p, C.POINTER(Shot), C.POINTER(C.c_int)]),
+    ("dc_gb300_batch_set_receivers", C.c_int,
+     [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_long)]),
+    ("dc_gb300_batch_set_tiles", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    ("dc_gb300_batch_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("dc_gb300_batch_autotune", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int), _fp]),
+    ("dc_gb300_batch_run", C.c_int, [C.c_void_p, C.c_int]),
+    ("dc_gb300_batch_synchronize", C.c_int, [C.c_void_p]),
+    ("dc_gb300_batch_get_fields", C.c_int, [C.c_void_p, C.c_int, _fp, _fp, _fp, _fp]),
+    ("dc_gb300_batch_get_traces", C.c_int, [C.c_void_p, C.c_int, C.c_int, _fp]),
+    ("dc_gb300_batch_steps_done", C.c_int, [C.c_void_p]),
+    ("dc_gb300_batch_kernel_launches", C.c_long, [C.c_void_p]),
+    ("dc_gb300_batch_stream", C.c_void_p, [C.c_void_p]),
+    ("dc_gb300_batch_points", C.c_longlong, [C.c_void_p]),
     ("dc_gb300_exact_steps_noalloc", C.c_int,
      [C.c_void_p, C.POINTER(C.c_void_p), C.c_void_p, C.c_int, _dp, C.c_void_p]),
     ("dc_gb300_source", C.c_float, [C.c_float, C.c_int, C.c_double]),
@@ -511,6 +543,117 @@ class Simulation:
     @property
     def device_data(self) -> int:
         return int(lib().dc_gb300_device_data(self.h))
+
+
+class Batch:
+    """Shots cropped out of one shared medium, advanced together
+    (dc_gb300_batch_create ... dc_gb300_batch_destroy).
+
+    ``medium_sizes`` are the medium box's (mx, my, mz); a shot is
+    ``add_shot(sizes, origin, src, fcut, absorb, kappa)`` with its padded box
+    sizes, the medium position of its point (0, 0, 0) (x a multiple of 4) and
+    its source in box coordinates."""
+
+    def __init__(self, medium_sizes, d=(12.5, 12.5, 12.5), dt=1e-3, medium=MEDIUM_PRECOMP,
+                 device=-1, max_steps=1000):
+        self.medium_sizes = tuple(int(v) for v in medium_sizes)
+        cfg = BatchConfig(*self.medium_sizes, d[0], d[1], d[2], dt, medium, device,
+                          int(max_steps))
+        h = C.c_void_p()
+        check(lib().dc_gb300_batch_create(C.byref(cfg), C.byref(h)))
+        self.h = h.value
+        self.shots = []
+        self.nrec = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().dc_gb300_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def generate_layered(self, spec: LayeredSpec) -> None:
+        check(lib().dc_gb300_batch_generate_layered(self.h, C.byref(spec)))
+
+    def set_precomp(self, coef) -> None:
+        mx, my, mz = self.medium_sizes
+        keep = [_f32(c).reshape(mz, my, mx) for c in coef]
+        pv = PrecompVars(*[fptr(c) for c in keep])
+        check(lib().dc_gb300_batch_set_precomp(self.h, C.byref(pv)))
+
+    def add_shot(self, sizes, origin, src, fcut=40.0, absorb=0, kappa=0.0) -> int:
+        sh = Shot(*[int(v) for v in sizes], *[int(v) for v in origin], *[int(v) for v in src],
+                  float(fcut), int(absorb), float(kappa))
+        idx = C.c_int(-1)
+        check(lib().dc_gb300_batch_add_shot(self.h, C.byref(sh), C.byref(idx)))
+        self.shots.append(tuple(int(v) for v in sizes))
+        self.nrec.append(0)
+        return idx.value
+
+    def set_receivers(self, shot: int, xyz) -> None:
+        a = np.ascontiguousarray(xyz, np.int64).reshape(-1, 3)
+        arr = (C.c_long * max(1, a.size))(*a.reshape(-1).tolist())
+        check(lib().dc_gb300_batch_set_receivers(self.h, int(shot), int(a.shape[0]), arr))
+        self.nrec[shot] = int(a.shape[0])
+
+    def set_tiles(self, ty: int, zsplit: int) -> None:
+        check(lib().dc_gb300_batch_set_tiles(self.h, int(ty), int(zsplit)))
+
+    def tiles(self):
+        ty, zs = C.c_int(), C.c_int()
+        check(lib().dc_gb300_batch_tiles(self.h, C.byref(ty), C.byref(zs)))
+        return ty.value, zs.value
+
+    def autotune(self, steps: int = 4):
+        """(ty, zsplit, ms per step) of the fastest tile candidate; leaves
+        the batch at step 0 with zero wavefields."""
+        ty, zs, ms = C.c_int(), C.c_int(), C.c_float()
+        check(lib().dc_gb300_batch_autotune(self.h, int(steps), C.byref(ty), C.byref(zs),
+                                            C.byref(ms)))
+        return ty.value, zs.value, ms.value
+
+    def run(self, steps: int) -> None:
+        check(lib().dc_gb300_batch_run(self.h, int(steps)))
+
+    def synchronize(self) -> None:
+        check(lib().dc_gb300_batch_synchronize(self.h))
+
+    def get_fields(self, shot: int):
+        sx, sy, sz = self.shots[shot]
+        out = [np.empty((sz, sy, sx), np.float32) for _ in range(4)]
+        check(lib().dc_gb300_batch_get_fields(self.h, int(shot), *[fptr(a) for a in out]))
+        return dict(zip(("pp", "pc", "qp", "qc"), out))
+
+    def traces(self, shot: int, steps: int) -> np.ndarray:
+        out = np.empty((steps, self.nrec[shot]), np.float32)
+        check(lib().dc_gb300_batch_get_traces(self.h, int(shot), int(steps), fptr(out)))
+        return out
+
+    @property
+    def steps_done(self) -> int:
+        return int(lib().dc_gb300_batch_steps_done(self.h))
+
+    @property
+    def launches(self) -> int:
+        return int(lib().dc_gb300_batch_kernel_launches(self.h))
+
+    @property
+    def stream(self) -> int:
+        return int(lib().dc_gb300_batch_stream(self.h) or 0)
+
+    @property
+    def points(self) -> int:
+        return int(lib().dc_gb300_batch_points(self.h))
 
 
 def header_symbols() -> list[str]:

@@ -96,6 +96,26 @@ struct StepParams {
   float *traces;
   int nrec, trace_cap, col_stride;
   int *err;
+  // position of the box's point (0, 0, 0) in the medium's arrays (the
+  // batched form crops shots out of one shared medium; 0 otherwise)
+  int mox, moy, moz;
+};
+
+// One launch of the batched fast kernel: up to kMaxBatchShots shots, each a
+// box with its own wavefields, source, sponge and receivers, cropped out of
+// one shared medium.  Work items are column tiles (x, y) x z-chunks of every
+// shot, numbered shot by shot; persistent CTAs stride over them.
+constexpr int kMaxBatchShots = 64;
+struct BatchLaunch {
+  CUtensorMap tm_l, tm_o1, tm_o2;  // shared medium (coefficient groups)
+  const CUtensorMap *maps;          // [shot][4]: halo of buffer 0, 1; own tile of buffer 0, 1
+  int nshots;
+  int cur_buf;                      // buffer holding (pc, qc) in every shot
+  int n_items;
+  int *err;
+  int item_prefix[kMaxBatchShots + 1];
+  int tiles_x[kMaxBatchShots], tiles_y[kMaxBatchShots];
+  StepParams shot[kMaxBatchShots];
 };
 
 struct Sim {
@@ -156,6 +176,23 @@ struct FastShape {
 };
 FastShape fast_shape(const Sim *sim);
 bool fast_encode_maps(Sim *sim, std::string *err);
+// Tile rows (TY) of the single-simulation fast kernel (8 unless
+// DC_GB300_FAST_TY=16).
+int fast_default_ty();
+// Tensor maps of one (p, q) pair buffer for tiles of 32 x ty: the halo box
+// (read as the current field) and the own tile (previous field).
+bool fast_encode_pair_maps(const float2 *buf, long long sx, long long sy, long long sz,
+                           long long pitch, int ty, CUtensorMap *halo, CUtensorMap *own,
+                           std::string *err);
+// Tensor maps of the three coefficient groups of a medium in form `form`.
+bool fast_encode_medium_maps(int form, const float *coef, const void *coef16, const float *vv,
+                             long long sx, long long sy, long long sz, long long pitch,
+                             long long count, int ty, CUtensorMap out[3], std::string *err);
+// Batched fast kernel (always with the sponge).  `blocks` = persistent CTAs.
+cudaError_t batch_prepare(int ty, int form);  // shared-memory attributes
+int batch_blocks_per_sm(int ty, int form, bool iso);
+cudaError_t launch_batch(cudaStream_t st, const BatchLaunch &bl, int ty, int form, bool iso,
+                         int blocks);
 
 // Launchers.  Return the cudaError_t of the launch.
 cudaError_t launch_fast(Sim *sim, const StepParams &prm, int cur_buf,
@@ -221,6 +258,10 @@ bool encode_tiled(CUtensorMap *map, const void *base, int rank,
                   const uint64_t *dims, const uint64_t *strides_bytes,
                   const uint32_t *box, std::string *err,
                   CUtensorMapDataType type = CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+
+// FD weights, inverse spacings, dt and dt^2 of a pass (the vexp scaling of
+// the narrow medium forms is applied by the caller).
+void fill_weights(StepParams *p, float dx, float dy, float dz, float dt);
 
 // Thread-local error text for dc_gb300_last_error().
 void set_error(const std::string &msg);

@@ -23,6 +23,12 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
 }
 
 // Makes the mbarrier initialisation visible to the async (TMA) proxy.
+// Invalidates an mbarrier whose phases have all completed, so that its
+// word can be initialised again.
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ void mbar_init_fence() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }

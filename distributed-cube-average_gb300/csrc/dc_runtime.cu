@@ -140,6 +140,38 @@ void release(Sim *s) {
   if (s->stream) cudaStreamDestroy(s->stream);
 }
 
+}  // namespace
+
+// FD weights, inverse spacings, dt and dt^2 of a pass.
+void fill_weights(StepParams *p, float dx, float dy, float dz, float dt) {
+  // include/sample_compute.h:40-45 (float, IEEE division)
+  p->dxxinv = 1.0f / (dx * dx);
+  p->dyyinv = 1.0f / (dy * dy);
+  p->dzzinv = 1.0f / (dz * dz);
+  p->dxyinv = 1.0f / (dx * dy);
+  p->dxzinv = 1.0f / (dx * dz);
+  p->dyzinv = 1.0f / (dy * dz);
+  {
+    const double K[5] = {-205.0 / 72.0, 8.0 / 5.0, -1.0 / 5.0, 8.0 / 315.0, -1.0 / 560.0};
+    const double L[4] = {4.0 / 5.0, -1.0 / 5.0, 4.0 / 105.0, -1.0 / 280.0};
+    const double hx = dx, hy = dy, hz = dz;
+    for (int k = 0; k < 5; ++k) {
+      p->w2x[k] = static_cast<float>(K[k] / (hx * hx));
+      p->w2y[k] = static_cast<float>(K[k] / (hy * hy));
+      p->w2z[k] = static_cast<float>(K[k] / (hz * hz));
+    }
+    for (int k = 0; k < 4; ++k) {
+      p->w1x[k] = static_cast<float>(L[k] / hx);
+      p->w1y[k] = static_cast<float>(L[k] / hy);
+      p->w1z[k] = static_cast<float>(L[k] / hz);
+    }
+  }
+  p->dt = dt;
+  p->dt2 = dt * dt;
+}
+
+namespace {
+
 // Fills the parameters of one stencil pass over a box.
 StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
                        float dx, float dy, float dz, float dt) {
@@ -155,30 +187,7 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
   p.zchunk = s->kernel == DC_GB300_KERNEL_FAST ? fast_shape(s).zchunk : kExactZChunk;
   p.pitch = s->pitch;
   p.plane = s->plane;
-  // include/sample_compute.h:40-45 (float, IEEE division)
-  p.dxxinv = 1.0f / (dx * dx);
-  p.dyyinv = 1.0f / (dy * dy);
-  p.dzzinv = 1.0f / (dz * dz);
-  p.dxyinv = 1.0f / (dx * dy);
-  p.dxzinv = 1.0f / (dx * dz);
-  p.dyzinv = 1.0f / (dy * dz);
-  {
-    const double K[5] = {-205.0 / 72.0, 8.0 / 5.0, -1.0 / 5.0, 8.0 / 315.0, -1.0 / 560.0};
-    const double L[4] = {4.0 / 5.0, -1.0 / 5.0, 4.0 / 105.0, -1.0 / 280.0};
-    const double hx = dx, hy = dy, hz = dz;
-    for (int k = 0; k < 5; ++k) {
-      p.w2x[k] = static_cast<float>(K[k] / (hx * hx));
-      p.w2y[k] = static_cast<float>(K[k] / (hy * hy));
-      p.w2z[k] = static_cast<float>(K[k] / (hz * hz));
-    }
-    for (int k = 0; k < 4; ++k) {
-      p.w1x[k] = static_cast<float>(L[k] / hx);
-      p.w1y[k] = static_cast<float>(L[k] / hy);
-      p.w1z[k] = static_cast<float>(L[k] / hz);
-    }
-  }
-  p.dt = dt;
-  p.dt2 = dt * dt;
+  fill_weights(&p, dx, dy, dz, dt);
   // the FP16/BF16 medium stores the velocity terms scaled by 2^-vexp
   if (s->coef_form == CF_F16 || s->coef_form == CF_BF16) p.dt2 = ldexpf(p.dt2, s->vexp);
   const dc_device_data &a = s->handle->abi;

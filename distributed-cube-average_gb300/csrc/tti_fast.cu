@@ -176,54 +176,49 @@ __device__ __forceinline__ OutMedium load_out(const unsigned char *o1, const uns
   return OutMedium{a.x, a.y, b.x, b.y, c.x, c.y};
 }
 
+// Sweeps the column tile at (x0, y0) over the output planes [zb, ze) of the
+// box in prm, with the CTA's shared memory `smem` (128-byte aligned).  The
+// FD weights, dt2 and the energy output are read from `cw`, the parameters
+// shared by every box of the launch (kept at fixed constant-bank offsets so
+// they feed the arithmetic directly).
+// Returns false if a TMA wait timed out: the error word is set and the
+// copies in flight have been given a bounded chance to land.
 template <int TX, int TY, int CF, bool SPONGE, bool ISO>
-__global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
-    fast_kernel(const __grid_constant__ CUtensorMap tm_cur,
-                const __grid_constant__ CUtensorMap tm_prev,
-                const __grid_constant__ CUtensorMap tm_l,
-                const __grid_constant__ CUtensorMap tm_o1,
-                const __grid_constant__ CUtensorMap tm_o2,
-                const __grid_constant__ StepParams prm) {
+__device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
+                                             const CUtensorMap *tm_prev,
+                                             const CUtensorMap *tm_l,
+                                             const CUtensorMap *tm_o1,
+                                             const CUtensorMap *tm_o2, const StepParams &prm,
+                                             const StepParams &cw, const int x0, const int y0, const int zb,
+                                             const int ze, unsigned char *smem) {
   using Lay = FastLayout<TX, TY, CF>;
   using CB = CoefBytes<CF>;
   constexpr int NSTAGE = Lay::NSTAGE;
   constexpr int HX = Lay::HX;
   constexpr int NT = Lay::NT;
   // equal spacing on all axes: one set of weights serves x, y and z
-  const float *w2x = prm.w2x, *w1x = prm.w1x;
-  const float *w2y = ISO ? prm.w2x : prm.w2y, *w1y = ISO ? prm.w1x : prm.w1y;
-  const float *w2z = ISO ? prm.w2x : prm.w2z, *w1z = ISO ? prm.w1x : prm.w1z;
-  // No static shared memory in this kernel: the dynamic window starts at
-  // the CTA's shared base, so this alignment holds and every access below
-  // is a shared-space access.
-  extern __shared__ __align__(1024) unsigned char smem[];
+  const float *w2x = cw.w2x, *w1x = cw.w1x;
+  const float *w2y = ISO ? cw.w2x : cw.w2y, *w1y = ISO ? cw.w1x : cw.w1y;
+  const float *w2z = ISO ? cw.w2x : cw.w2z, *w1z = ISO ? cw.w1x : cw.w1z;
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + Lay::OFF_BAR);
 
   const int tid = threadIdx.x;
   const int tx = tid % TX, ty = tid / TX;
-  const int x0 = prm.tile_x0 + static_cast<int>(blockIdx.x) * TX;
-  const int y0 = prm.tile_y0 + static_cast<int>(blockIdx.y) * TY;
-  const int zb = prm.z0 + static_cast<int>(blockIdx.z) * prm.zchunk;
-  const int ze = min(zb + prm.zchunk, prm.z1);
   const int n_it = ze - zb + 2 * kHalo;
   const int gx = x0 + tx, gy = y0 + ty;
   const bool active =
       gx >= prm.x0 && gx < prm.x1 && gy >= prm.y0 && gy < prm.y1;
+  // medium coordinates of the tile
+  const int mx0 = x0 + prm.mox, my0 = y0 + prm.moy;
 
-  // TMA destinations must be 128-byte aligned; refuse to run otherwise
-  // (CTA-uniform, before any copy is issued).
-  if (smem_u32(smem) & 127u) {
-    if (tid == 0) atomicOr(prm.err, kErrAlign);
-    return;
-  }
   if (tid == 0) {
     for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
     mbar_init_fence();
-    prefetch_tensormap(&tm_cur);
-    prefetch_tensormap(&tm_prev);
-    if (CB::L) prefetch_tensormap(&tm_l);
-    prefetch_tensormap(&tm_o1);
-    if (CB::O2) prefetch_tensormap(&tm_o2);
+    prefetch_tensormap(tm_cur);
+    prefetch_tensormap(tm_prev);
+    if (CB::L) prefetch_tensormap(tm_l);
+    prefetch_tensormap(tm_o1);
+    if (CB::O2) prefetch_tensormap(tm_o2);
   }
   __syncthreads();
 
@@ -236,23 +231,24 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     const bool want_out = j >= 2 * kHalo;
     mbar_arrive_expect_tx(&bars[s], Lay::TX_HALO + (want_lead ? Lay::TX_LEAD : 0u) +
                                         (want_out ? Lay::TX_OUT : 0u));
-    tma_load_3d(st + Lay::OFF_H, &tm_cur, x0 - kHalo, y0 - kHalo, k, &bars[s]);
+    tma_load_3d(st + Lay::OFF_H, tm_cur, x0 - kHalo, y0 - kHalo, k, &bars[s]);
     // 16-byte groups are 4-D boxes (4 x 4-byte lanes innermost), 8- and
     // 4-byte groups 3-D boxes of one element per point
     if (want_lead) {
       if (CB::L == 16)
-        tma_load_4d(st + Lay::OFF_L, &tm_l, 0, x0, y0, k, &bars[s]);
+        tma_load_4d(st + Lay::OFF_L, tm_l, 0, mx0, my0, k + prm.moz, &bars[s]);
       else
-        tma_load_3d(st + Lay::OFF_L, &tm_l, x0, y0, k, &bars[s]);
+        tma_load_3d(st + Lay::OFF_L, tm_l, mx0, my0, k + prm.moz, &bars[s]);
     }
     if (want_out) {
       const int z = k - kHalo;
+      const int mz = z + prm.moz;
       if (CB::O1 == 16)
-        tma_load_4d(st + Lay::OFF_O1, &tm_o1, 0, x0, y0, z, &bars[s]);
+        tma_load_4d(st + Lay::OFF_O1, tm_o1, 0, mx0, my0, mz, &bars[s]);
       else
-        tma_load_3d(st + Lay::OFF_O1, &tm_o1, x0, y0, z, &bars[s]);
-      if (CB::O2) tma_load_3d(st + Lay::OFF_O2, &tm_o2, x0, y0, z, &bars[s]);
-      tma_load_3d(st + Lay::OFF_OWN, &tm_prev, x0, y0, z, &bars[s]);
+        tma_load_3d(st + Lay::OFF_O1, tm_o1, mx0, my0, mz, &bars[s]);
+      if (CB::O2) tma_load_3d(st + Lay::OFF_O2, tm_o2, mx0, my0, mz, &bars[s]);
+      tma_load_3d(st + Lay::OFF_OWN, tm_prev, x0, y0, z, &bars[s]);
     }
   };
 
@@ -381,14 +377,14 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
           float2 nv;
           if (SPONGE) {
             const float g = gxy * gzv;
-            nv = mul2(fma2(rhs, bc(prm.dt2), fma2(bc(-g), pv, cc)), bc(g));
+            nv = mul2(fma2(rhs, bc(cw.dt2), fma2(bc(-g), pv, cc)), bc(g));
           } else {
-            nv = fma2(rhs, bc(prm.dt2), fma2(bc(-1.0f), pv, cc));
+            nv = fma2(rhs, bc(cw.dt2), fma2(bc(-1.0f), pv, cc));
           }
           const int z = zb + it - 2 * kHalo;
           if (SPONGE && z + 1 < ze) gzv = prm.sponge[prm.sponge_oz + z + 1];
           if (active) {
-            if (prm.energy) e_acc = fma2(nv, nv, e_acc);
+            if (cw.energy) e_acc = fma2(nv, nv, e_acc);
             if (z == ev) {  // a receiver and/or the source sits at this point
               const int step = *prm.d_step + prm.step_offset;
               while (z == rnext) {
@@ -426,9 +422,9 @@ done:
         mbar_wait_bounded(&bars[j % NSTAGE],
                           static_cast<uint32_t>(j / NSTAGE) & 1u, kWaitLimitNs);
     }
-    return;
+    return false;
   }
-  if (prm.energy) {
+  if (cw.energy) {
     // CTA reduction of the float partials in double, one atomic per CTA.
     double e = static_cast<double>(e_acc.x) + static_cast<double>(e_acc.y);
 #pragma unroll
@@ -441,8 +437,75 @@ done:
       double tot = 0.0;
       for (int w = 0; w < NT / 32; ++w) tot += red[w];
       const int step = *prm.d_step + prm.step_offset;
-      if (step >= 0 && step < prm.energy_cap) atomicAdd(&prm.energy[step], tot);
+      if (step >= 0 && step < cw.energy_cap) atomicAdd(&cw.energy[step], tot);
     }
+  }
+  // every copy of this column has landed and been read: release the
+  // barriers so the CTA can initialise them again for its next column
+  __syncthreads();
+  if (tid == 0)
+    for (int s = 0; s < NSTAGE; ++s) mbar_inval(&bars[s]);
+  return true;
+}
+
+// No static shared memory in these kernels: the dynamic window starts at
+// the CTA's shared base, so the 1024-byte alignment holds and every access
+// is a shared-space access.  TMA destinations must be 128-byte aligned; the
+// kernels refuse to run otherwise (CTA-uniform, before any copy is issued).
+
+// One pass over a box: CTA (bx, by, bz) sweeps tile (bx, by), z-chunk bz.
+template <int TX, int TY, int CF, bool SPONGE, bool ISO>
+__global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
+    fast_kernel(const __grid_constant__ CUtensorMap tm_cur,
+                const __grid_constant__ CUtensorMap tm_prev,
+                const __grid_constant__ CUtensorMap tm_l,
+                const __grid_constant__ CUtensorMap tm_o1,
+                const __grid_constant__ CUtensorMap tm_o2,
+                const __grid_constant__ StepParams prm) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  if (smem_u32(smem) & 127u) {
+    if (threadIdx.x == 0) atomicOr(prm.err, kErrAlign);
+    return;
+  }
+  const int x0 = prm.tile_x0 + static_cast<int>(blockIdx.x) * TX;
+  const int y0 = prm.tile_y0 + static_cast<int>(blockIdx.y) * TY;
+  const int zb = prm.z0 + static_cast<int>(blockIdx.z) * prm.zchunk;
+  const int ze = min(zb + prm.zchunk, prm.z1);
+  sweep_column<TX, TY, CF, SPONGE, ISO>(&tm_cur, &tm_prev, &tm_l, &tm_o1, &tm_o2, prm, prm, x0,
+                                        y0, zb, ze, smem);
+}
+
+// One step of a batch of shots: persistent CTAs stride over the work items
+// (shot by shot: x tile fastest, then y tile, then z-chunk).  The shot of an
+// item is found from the per-shot prefix counts, so every index here is
+// CTA-uniform.
+template <int TX, int TY, int CF, bool ISO>
+__global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
+    batch_kernel(const __grid_constant__ BatchLaunch bl) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  if (smem_u32(smem) & 127u) {
+    if (threadIdx.x == 0) atomicOr(bl.err, kErrAlign);
+    return;
+  }
+  for (int item = blockIdx.x; item < bl.n_items; item += gridDim.x) {
+    int s = 0;
+    while (s + 1 < bl.nshots && bl.item_prefix[s + 1] <= item) ++s;
+    const StepParams &prm = bl.shot[s];
+    int local = item - bl.item_prefix[s];
+    const int ix = local % bl.tiles_x[s];
+    local /= bl.tiles_x[s];
+    const int iy = local % bl.tiles_y[s];
+    const int iz = local / bl.tiles_y[s];
+    const int x0 = prm.tile_x0 + ix * TX, y0 = prm.tile_y0 + iy * TY;
+    const int zb = prm.z0 + iz * prm.zchunk;
+    const int ze = min(zb + prm.zchunk, prm.z1);
+    const CUtensorMap *m = bl.maps + 4 * s;
+    // weights, dt2 and energy (none) are the same in every shot: read them
+    // from shot 0 at fixed offsets
+    if (!sweep_column<TX, TY, CF, true, ISO>(m + bl.cur_buf, m + 2 + (1 - bl.cur_buf),
+                                             &bl.tm_l, &bl.tm_o1, &bl.tm_o2, prm, bl.shot[0],
+                                             x0, y0, zb, ze, smem))
+      return;
   }
 }
 
@@ -532,6 +595,59 @@ FastShape fast_shape(const Sim *sim) {
   return FastShape{kTX, ty, static_cast<int>(zc)};
 }
 
+int fast_default_ty() { return chosen_ty(); }
+
+bool fast_encode_pair_maps(const float2 *buf, long long sx, long long sy, long long sz,
+                           long long pitch, int ty, CUtensorMap *halo, CUtensorMap *own,
+                           std::string *err) {
+  const uint64_t dims3[3] = {static_cast<uint64_t>(sx), static_cast<uint64_t>(sy),
+                             static_cast<uint64_t>(sz)};
+  // (p, q) pair buffers: 8-byte elements
+  const uint64_t str8[2] = {static_cast<uint64_t>(pitch) * 8,
+                            static_cast<uint64_t>(pitch * sy) * 8};
+  const uint32_t box_halo[3] = {kTX + 8, static_cast<uint32_t>(ty) + 8, 1};
+  const uint32_t box_tile[3] = {kTX, static_cast<uint32_t>(ty), 1};
+  const auto U64 = CU_TENSOR_MAP_DATA_TYPE_UINT64;
+  return encode_tiled(halo, buf, 3, dims3, str8, box_halo, err, U64) &&
+         encode_tiled(own, buf, 3, dims3, str8, box_tile, err, U64);
+}
+
+bool fast_encode_medium_maps(int form, const float *coef, const void *coef16, const float *vv,
+                             long long sx, long long sy, long long sz, long long pitch,
+                             long long count, int ty, CUtensorMap out[3], std::string *err) {
+  const uint64_t X = sx, Y = sy, Z = sz, P = pitch, PL = pitch * sy;
+  const uint64_t dims3[3] = {X, Y, Z};
+  const uint64_t str8[2] = {P * 8, PL * 8};
+  const uint64_t str4[2] = {P * 4, PL * 4};
+  const uint32_t box_tile[3] = {kTX, static_cast<uint32_t>(ty), 1};
+  // 16-byte coefficient groups: 4 lanes of 4 bytes innermost
+  const uint64_t dims4[4] = {4, X, Y, Z};
+  const uint64_t str16[3] = {16, P * 16, PL * 16};
+  const uint32_t box16[4] = {4, kTX, static_cast<uint32_t>(ty), 1};
+  const auto U64 = CU_TENSOR_MAP_DATA_TYPE_UINT64, U32 = CU_TENSOR_MAP_DATA_TYPE_UINT32;
+  const auto F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  const long long cnt = count;
+  // out[0] = L (cxx, cyy, cxy, czz), out[1] = O1, out[2] = O2
+  switch (form) {
+    case CF_F32: {
+      const char *c = reinterpret_cast<const char *>(coef);
+      return encode_tiled(&out[0], c, 4, dims4, str16, box16, err, F32) &&
+             encode_tiled(&out[1], c + cnt * 16, 4, dims4, str16, box16, err, F32) &&
+             encode_tiled(&out[2], c + cnt * 32, 3, dims3, str8, box_tile, err, U64);
+    }
+    case CF_VV:
+      if (!encode_tiled(&out[1], vv, 3, dims3, str8, box_tile, err, U64)) return false;
+      out[0] = out[2] = out[1];  // unused
+      return true;
+    default: {  // CF_F16, CF_BF16: 8-byte L, 8-byte O1, 4-byte O2
+      const char *h = static_cast<const char *>(coef16);
+      return encode_tiled(&out[0], h, 3, dims3, str8, box_tile, err, U64) &&
+             encode_tiled(&out[1], h + cnt * 8, 3, dims3, str8, box_tile, err, U64) &&
+             encode_tiled(&out[2], h + cnt * 16, 3, dims3, str4, box_tile, err, U32);
+    }
+  }
+}
+
 bool fast_encode_maps(Sim *sim, std::string *err) {
   // dynamic shared memory above 48 KB must be enabled per kernel and device
   // (done here, before any stream capture)
@@ -541,50 +657,103 @@ bool fast_encode_maps(Sim *sim, std::string *err) {
     *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(ae);
     return false;
   }
-  const uint64_t X = sim->sx, Y = sim->sy, Z = sim->sz;
-  const uint64_t P = sim->pitch, PL = sim->plane;
-  const uint64_t dims3[3] = {X, Y, Z};
-  // (p, q) pair buffers: 8-byte elements
-  const uint64_t str8[2] = {P * 8, PL * 8};
-  const uint32_t box_halo[3] = {kTX + 8, static_cast<uint32_t>(kTY) + 8, 1};
-  const uint32_t box_tile[3] = {kTX, static_cast<uint32_t>(kTY), 1};
-  const auto U64 = CU_TENSOR_MAP_DATA_TYPE_UINT64, U32 = CU_TENSOR_MAP_DATA_TYPE_UINT32;
-  const auto F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-  for (int b = 0; b < 2; ++b) {
-    if (!encode_tiled(&sim->tm_halo[b], sim->pq[b], 3, dims3, str8, box_halo, err, U64))
+  for (int b = 0; b < 2; ++b)
+    if (!fast_encode_pair_maps(sim->pq[b], sim->sx, sim->sy, sim->sz, sim->pitch, kTY,
+                               &sim->tm_halo[b], &sim->tm_own[b], err))
       return false;
-    if (!encode_tiled(&sim->tm_own[b], sim->pq[b], 3, dims3, str8, box_tile, err, U64))
-      return false;
-  }
-  // 16-byte coefficient groups: 4 lanes of 4 bytes innermost
-  const uint64_t dims4[4] = {4, X, Y, Z};
-  const uint64_t str16[3] = {16, P * 16, PL * 16};
-  const uint32_t box16[4] = {4, kTX, static_cast<uint32_t>(kTY), 1};
-  const uint64_t str4[2] = {P * 4, PL * 4};
-  const char *c = reinterpret_cast<const char *>(sim->coef);
-  const long long cnt = sim->count;
-  // tm_c[0] = L (cxx, cyy, cxy, czz), tm_c[1] = O1, tm_c[2] = O2
-  switch (sim->coef_form) {
-    case CF_F32:
-      if (!encode_tiled(&sim->tm_c[0], c, 4, dims4, str16, box16, err, F32)) return false;
-      if (!encode_tiled(&sim->tm_c[1], c + cnt * 16, 4, dims4, str16, box16, err, F32)) return false;
-      if (!encode_tiled(&sim->tm_c[2], c + cnt * 32, 3, dims3, str8, box_tile, err, U64)) return false;
-      break;
-    case CF_VV:
-      if (!encode_tiled(&sim->tm_c[1], sim->vv, 3, dims3, str8, box_tile, err, U64)) return false;
-      sim->tm_c[0] = sim->tm_c[2] = sim->tm_c[1];  // unused
-      break;
-    default: {  // CF_F16, CF_BF16: 8-byte L, 8-byte O1, 4-byte O2
-      const char *h = static_cast<const char *>(sim->coef16);
-      if (!encode_tiled(&sim->tm_c[0], h, 3, dims3, str8, box_tile, err, U64)) return false;
-      if (!encode_tiled(&sim->tm_c[1], h + cnt * 8, 3, dims3, str8, box_tile, err, U64)) return false;
-      if (!encode_tiled(&sim->tm_c[2], h + cnt * 16, 3, dims3, str4, box_tile, err, U32))
-        return false;
-    }
-  }
+  if (!fast_encode_medium_maps(sim->coef_form, sim->coef, sim->coef16, sim->vv, sim->sx, sim->sy,
+                               sim->sz, sim->pitch, sim->count, kTY, sim->tm_c, err))
+    return false;
   sim->maps_tx = kTX;
   sim->maps_ty = kTY;
   return true;
+}
+
+namespace {
+
+template <int TY, int CF, bool ISO>
+cudaError_t batch_attr() {
+  return cudaFuncSetAttribute(batch_kernel<kTX, TY, CF, ISO>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              FastLayout<kTX, TY, CF>::SMEM_BYTES);
+}
+
+template <int TY, int CF>
+cudaError_t batch_attr_cf() {
+  cudaError_t e = batch_attr<TY, CF, false>();
+  return e == cudaSuccess ? batch_attr<TY, CF, true>() : e;
+}
+
+template <int TY>
+cudaError_t batch_attr_ty(int form) {
+  switch (form) {
+    case CF_F16: return batch_attr_cf<TY, CF_F16>();
+    case CF_BF16: return batch_attr_cf<TY, CF_BF16>();
+    case CF_VV: return batch_attr_cf<TY, CF_VV>();
+    default: return batch_attr_cf<TY, CF_F32>();
+  }
+}
+
+template <int TY, int CF, bool ISO>
+int batch_occ() {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<kTX, TY, CF, ISO>, kTX * TY,
+                                                    FastLayout<kTX, TY, CF>::SMEM_BYTES) !=
+      cudaSuccess)
+    return 0;
+  return n;
+}
+
+template <int TY, int CF>
+int batch_occ_cf(bool iso) {
+  return iso ? batch_occ<TY, CF, true>() : batch_occ<TY, CF, false>();
+}
+
+template <int TY>
+int batch_occ_ty(int form, bool iso) {
+  switch (form) {
+    case CF_F16: return batch_occ_cf<TY, CF_F16>(iso);
+    case CF_BF16: return batch_occ_cf<TY, CF_BF16>(iso);
+    case CF_VV: return batch_occ_cf<TY, CF_VV>(iso);
+    default: return batch_occ_cf<TY, CF_F32>(iso);
+  }
+}
+
+template <int TY, int CF>
+cudaError_t launch_batch_cf(cudaStream_t st, const BatchLaunch &bl, bool iso, int blocks) {
+  const int smem = FastLayout<kTX, TY, CF>::SMEM_BYTES;
+  if (iso)
+    batch_kernel<kTX, TY, CF, true><<<blocks, kTX * TY, smem, st>>>(bl);
+  else
+    batch_kernel<kTX, TY, CF, false><<<blocks, kTX * TY, smem, st>>>(bl);
+  return cudaGetLastError();
+}
+
+template <int TY>
+cudaError_t launch_batch_ty(cudaStream_t st, const BatchLaunch &bl, int form, bool iso,
+                            int blocks) {
+  switch (form) {
+    case CF_F16: return launch_batch_cf<TY, CF_F16>(st, bl, iso, blocks);
+    case CF_BF16: return launch_batch_cf<TY, CF_BF16>(st, bl, iso, blocks);
+    case CF_VV: return launch_batch_cf<TY, CF_VV>(st, bl, iso, blocks);
+    default: return launch_batch_cf<TY, CF_F32>(st, bl, iso, blocks);
+  }
+}
+
+}  // namespace
+
+cudaError_t batch_prepare(int ty, int form) {
+  return ty == 16 ? batch_attr_ty<16>(form) : batch_attr_ty<8>(form);
+}
+
+int batch_blocks_per_sm(int ty, int form, bool iso) {
+  return ty == 16 ? batch_occ_ty<16>(form, iso) : batch_occ_ty<8>(form, iso);
+}
+
+cudaError_t launch_batch(cudaStream_t st, const BatchLaunch &bl, int ty, int form, bool iso,
+                         int blocks) {
+  return ty == 16 ? launch_batch_ty<16>(st, bl, form, iso, blocks)
+                  : launch_batch_ty<8>(st, bl, form, iso, blocks);
 }
 
 cudaError_t launch_fast(Sim *sim, const StepParams &prm, int cur_buf, int prev_buf) {

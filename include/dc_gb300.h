@@ -358,6 +358,66 @@ float dc_gb300_source(float dt, int it, double fcut);
  * physical interior .. a next to the halo), 1 elsewhere. */
 void dc_gb300_sponge_profile(long s, long a, double kappa, float *g);
 
+/* ---- Part 3: batched shots over one shared medium (no counterpart in the
+ * reference, whose time loop src/worker.c:466-511 advances one shot) ----
+ *
+ * A batch holds one medium box and any number of shots.  A shot is a box
+ * cropped out of the medium, with its own (p, q) wavefields, wavelet, sponge
+ * and receivers, stepped exactly as a dc_gb300_sim with the fast kernel
+ * steps its cube (bit-identical fields for the same cropped medium).  One
+ * step of all shots is one launch of a persistent kernel per 64 shots;
+ * runs are captured into CUDA graphs. */
+typedef struct dc_gb300_batch dc_gb300_batch;
+
+typedef struct {
+  long mx, my, mz;          /* medium box sizes (x fastest) */
+  float dx, dy, dz, dt;
+  int medium;               /* DC_GB300_MEDIUM_PRECOMP, _PRECOMP_F16 or _PRECOMP_BF16 */
+  int device;               /* CUDA ordinal; -1 = current */
+  int max_steps;            /* capacity of wavelet tables and traces */
+} dc_gb300_batch_config;
+
+typedef struct {
+  long sx, sy, sz;          /* padded sizes of the shot box (>= 9) */
+  long ox, oy, oz;          /* medium position of the box's point (0, 0, 0); ox % 4 == 0 */
+  long src_x, src_y, src_z; /* source in box coordinates, inside [4, s-4)^3 */
+  double fcut;              /* wavelet cut-off frequency (Ricker peak fcut / 3) */
+  long absorb;              /* sponge width in cells (0: none) */
+  double kappa;             /* sponge strength (dc_gb300_sponge_profile) */
+} dc_gb300_shot;
+
+int dc_gb300_batch_create(const dc_gb300_batch_config *cfg, dc_gb300_batch **out);
+int dc_gb300_batch_destroy(dc_gb300_batch *batch);
+/* Medium of the whole box: the layered generator, or dense host arrays of
+ * mx*my*mz coefficients in the reference's precomp layout. */
+int dc_gb300_batch_generate_layered(dc_gb300_batch *batch, const dc_gb300_layered_spec *spec);
+int dc_gb300_batch_set_precomp(dc_gb300_batch *batch, const dc_precomp_vars *vars);
+/* Adds a shot with zero wavefields; *index receives its number. */
+int dc_gb300_batch_add_shot(dc_gb300_batch *batch, const dc_gb300_shot *shot, int *index);
+/* Receivers of one shot as (x, y, z) triples in box coordinates; traces
+ * (p before the next step's source, [step][receiver]) restart from zero. */
+int dc_gb300_batch_set_receivers(dc_gb300_batch *batch, int shot, int count, const long *xyz);
+/* Tile rows (8 or 16) and z-chunks per column (1..64). */
+int dc_gb300_batch_set_tiles(dc_gb300_batch *batch, int ty, int zsplit);
+int dc_gb300_batch_tiles(const dc_gb300_batch *batch, int *ty, int *zsplit);
+/* Times every tile candidate for `steps` steps on this batch, keeps the
+ * fastest (ms per step in *ms) and returns the batch to step 0 with zero
+ * wavefields and traces: call it before the first run. */
+int dc_gb300_batch_autotune(dc_gb300_batch *batch, int steps, int *ty, int *zsplit, float *ms);
+/* Queues `steps` steps of every shot (asynchronous on the batch's stream). */
+int dc_gb300_batch_run(dc_gb300_batch *batch, int steps);
+int dc_gb300_batch_synchronize(dc_gb300_batch *batch);
+/* Dense sx*sy*sz fields of one shot (any pointer may be NULL); the same
+ * observable state as a dc_gb300_sim after the same steps.  Synchronous. */
+int dc_gb300_batch_get_fields(dc_gb300_batch *batch, int shot, float *pp, float *pc, float *qp,
+                              float *qc);
+int dc_gb300_batch_get_traces(dc_gb300_batch *batch, int shot, int steps, float *out);
+int dc_gb300_batch_steps_done(const dc_gb300_batch *batch);
+long dc_gb300_batch_kernel_launches(const dc_gb300_batch *batch);
+void *dc_gb300_batch_stream(dc_gb300_batch *batch);
+/* Updated points per step summed over the shots ((s-8) per axis). */
+long long dc_gb300_batch_points(const dc_gb300_batch *batch);
+
 /* Runs `steps` time steps of the exact kernel (reference arithmetic, no
  * source, no sponge) over caller-owned device buffers and allocates no
  * device memory.  No counterpart in the reference: it serves callers that
