@@ -1,8 +1,9 @@
 """Benchmark of the Fletcher TTI time step on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--form plain|batched] [--medium f32|f16|bf16]
 
-Workload (BASELINE configs[1]): 512^3 interior + 48-cell absorbing shell
+Plain workload: 512^3 interior + 48-cell absorbing shell
 (616^3 padded, 608^3 = 224.8 M updated points per step), dt = 0.8 ms,
 dx = dy = dz = 12.5 m, seeded 12-layer medium (numpy PCG64 seed 2026) on the
 GPU, 20 Hz Ricker (FCUT = 60) at interior depth 20, 48-cell sponge.  A step
@@ -21,6 +22,16 @@ step, dc_device_data_get_results), wall clock.  ``roofline`` compares the
 stencil kernel's algorithmic bytes (64 B per update) per launch time with the
 measured HBM copy bandwidth; ``cpu_baseline`` times the CPU oracle on a
 bounded slab of the same workload.
+
+Batched form (--form batched): 64 shots over one shared seeded medium of
+768 x 768 x 512 cells (plus a 52-cell margin per side for the shots'
+absorbing layers and halos: an 872 x 872 x 616 medium box), each shot a
+crop of U(192, 320) x U(192, 320) x 256 interior cells around its source
+(sources on an 8 x 8 surface grid with seeded jitter, depth 20, Ricker peak
+U(15, 25) Hz), a 48-cell sponge per shot, FP16 medium storage, 64 receivers
+per shot; tile rows and z-split chosen by the library's autotuner.  One step
+advances every shot (one persistent launch); K defaults to 1000 steps.
+``value`` is shot-point-updates per second summed over the shots.
 
 Reference arm (--impl reference): the reference's CPU implementation of the
 path (the oracle port of src/openmp_propagate.c, all host threads) on the
@@ -53,12 +64,20 @@ MEDIUM_SEED = 2026
 SPONGE_KAPPA = 0.35
 BYTES_PER_UPDATE = 64  # pc,qc,pp,qp + 10 coefficients read, pp,qp written
 SLAB_PLANES = 16       # CPU sample: planes per step
+# batched form
+BATCH_MODEL = (768, 768, 512)
+BATCH_PAD = ABSORB + 4  # sponge + halo around every crop
+BATCH_SHOTS = 64
+BATCH_DEPTH = 256
+BATCH_SEED = 2027
+BATCH_RECEIVERS = 64
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 2000 plain, 1000 batched)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--kernel", choices=("fast", "exact"), default="fast")
@@ -67,7 +86,12 @@ def parse():
     ap.add_argument("--n", type=int, default=N_INTERIOR, help="interior cells per axis")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--form", choices=("plain", "batched"), default="plain")
+    ap.add_argument("--shots", type=int, default=BATCH_SHOTS)
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 1000 if args.form == "batched" else 2000
+    return args
 
 
 def dist_env():
@@ -438,11 +462,133 @@ def run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_over_ran
                                   "dc_device_data_get_results), pinned host buffers"}
 
 
+def batch_shots(n_shots: int, seed: int = BATCH_SEED):
+    """Shot layout of the batched workload: sources on an 8 x 8 grid over the
+    model surface with seeded jitter; each shot a crop of uneven aperture
+    around its source.  Returns a list of dicts in medium-box coordinates."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    mx, my, mz = BATCH_MODEL
+    side = 8
+    shots = []
+    for k in range(n_shots):
+        i, j = (k % (side * side)) % side, (k % (side * side)) // side
+        sx_m = int(mx * (i + 0.5) / side + rng.uniform(-mx / side / 4, mx / side / 4))
+        sy_m = int(my * (j + 0.5) / side + rng.uniform(-my / side / 4, my / side / 4))
+        ax, ay = (int(v) for v in rng.integers(192, 321, size=2))
+        peak = float(rng.uniform(15.0, 25.0))
+        cx = min(max(sx_m - ax // 2, 0), mx - ax) // 4 * 4
+        cy = min(max(sy_m - ay // 2, 0), my - ay)
+        p = BATCH_PAD
+        sizes = (ax + 2 * p, ay + 2 * p, BATCH_DEPTH + 2 * p)
+        src = (sx_m - cx + p, sy_m - cy + p, p + SRC_DEPTH)
+        rec_x = np.linspace(p, p + ax - 1, BATCH_RECEIVERS).astype(int)
+        rec = [(int(x), src[1], p + 8) for x in rec_x]
+        shots.append({"sizes": sizes, "origin": (cx, cy, 0), "src": src, "fcut": 3.0 * peak,
+                      "rec": rec})
+    return shots
+
+
+def run_batched(args, rank, world, local):
+    """The batched form: all shots in one persistent, graph-captured launch
+    per step.  Ranks > 0 run their own independent batch (weak scaling)."""
+    import torch
+    import __graft_entry__ as ge
+    dc = ge.package()
+    dc.build()
+    from dc_gb300 import medium
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    form = {"f32": dc.MEDIUM_PRECOMP, "f16": dc.MEDIUM_PRECOMP_F16,
+            "bf16": dc.MEDIUM_PRECOMP_BF16}[args.medium if args.medium != "f32" else "f16"]
+    storage = "f16" if args.medium == "f32" else args.medium
+    mbox = tuple(v + 2 * BATCH_PAD for v in BATCH_MODEL)
+    shots = batch_shots(args.shots, BATCH_SEED + rank)
+    total = args.warmup + args.steps
+    b = dc.Batch(mbox, (DX,) * 3, DT, medium=form, device=local, max_steps=total + 1)
+    b.generate_layered(medium.layered_spec(MEDIUM_SEED, mbox))
+    for k, sh in enumerate(shots):
+        b.add_shot(sh["sizes"], sh["origin"], sh["src"], sh["fcut"], ABSORB, SPONGE_KAPPA)
+        b.set_receivers(k, sh["rec"])
+    ty, zsplit, tune_ms = b.autotune(3)
+    pts = b.points
+    b.run(args.warmup)
+    b.synchronize()
+    stream = torch.cuda.ExternalStream(b.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = b.launches
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        b.run(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    b.synchronize()
+    launches = b.launches - l0
+    ms = ev0.elapsed_time(ev1)
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    tr = b.traces(0, total)
+    assert np.isfinite(tr).all()
+    b.close()
+    value = pts * args.steps * world / (ms * 1e-3) / 1e9
+    bytes_per_update = 44 if storage in ("f16", "bf16") else 64
+    achieved = bytes_per_update * pts / (ms / args.steps * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle.oracle import Port
+        port = Port()
+        nthreads = os.cpu_count() or 1
+        ssizes, coef, fields = slab_inputs(dc, port, geometry(N_INTERIOR), SLAB_PLANES)
+        rate, reps, el = time_cpu_oracle(port, ssizes, coef, fields, 12.0, nthreads)
+        cpu = {"value": rate / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"{reps} oracle steps of a {ssizes[0] - 8}x{ssizes[1] - 8}x"
+                         f"{ssizes[2] - 8} slab of the plain workload ({el:.1f} s); the "
+                         "per-update CPU cost does not depend on the batching"}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded 12-layer TTI medium, numpy PCG64 seed 2026, generated on "
+                "GPU; shot layout PCG64 seed 2027)",
+        "config": {"workload": f"batched: {args.shots} shots in one persistent launch per step "
+                               f"over a shared {BATCH_MODEL[0]}x{BATCH_MODEL[1]}x"
+                               f"{BATCH_MODEL[2]} medium, crops U(192,320)^2 x {BATCH_DEPTH} "
+                               f"+ {ABSORB}-cell sponge, dt 0.8 ms, 15-25 Hz Ricker",
+                   "form": "batched", "medium_storage": storage, "shots": args.shots,
+                   "points_per_step": pts, "tiles": {"ty": ty, "zsplit": zsplit,
+                                                     "autotune_ms_per_step": tune_ms},
+                   "global_batch": args.shots * world, "seq_len": None,
+                   "parallelism": f"shots{args.shots}x{world}",
+                   "l2": "inputs ~76 GB >> 129 MB L2; no flush"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "bytes_per_update": bytes_per_update, "traffic": None},
+        "cpu_baseline": cpu,
+        "e2e": None,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.form == "batched":
+        run_batched(args, rank, world, local)
         return
     run_ours(args, rank, world, local)
 

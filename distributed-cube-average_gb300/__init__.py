@@ -197,6 +197,26 @@ SIGNATURES = [
     ("dc_gb300_batch_kernel_launches", C.c_long, [C.c_void_p]),
     ("dc_gb300_batch_stream", C.c_void_p, [C.c_void_p]),
     ("dc_gb300_batch_points", C.c_longlong, [C.c_void_p]),
+    ("dc_gb300_mlp_create", C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    ("dc_gb300_mlp_destroy", C.c_int, [C.c_void_p]),
+    ("dc_gb300_mlp_init", C.c_int, [C.c_void_p, C.c_uint]),
+    ("dc_gb300_mlp_set_params", C.c_int, [C.c_void_p, _fp]),
+    ("dc_gb300_mlp_get_params", C.c_int, [C.c_void_p, _fp]),
+    ("dc_gb300_mlp_device_params", C.c_void_p, [C.c_void_p]),
+    ("dc_gb300_mlp_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]),
+    ("dc_gb300_mlp_gradient", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, _fp,
+                                        _dp]),
+    ("dc_gb300_mlp_train", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_int,
+                                     C.c_int, C.c_float, C.c_ulonglong, _fp]),
+    ("dc_gb300_layer_cells", C.c_longlong, [C.c_long, C.c_long, C.c_long, C.c_int,
+                                           C.POINTER(C.c_int), C.c_longlong]),
+    ("dc_gb300_set_learned_layer", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    ("dc_gb300_lb_sample", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_long), C.c_int,
+                                     C.c_void_p, C.c_void_p, C.c_longlong,
+                                     C.POINTER(C.c_longlong)]),
+    ("dc_gb300_lb_rollout", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_long), C.c_int,
+                                      C.c_void_p, C.c_void_p, C.c_longlong,
+                                      C.POINTER(C.c_longlong)]),
     ("dc_gb300_exact_steps_noalloc", C.c_int,
      [C.c_void_p, C.POINTER(C.c_void_p), C.c_void_p, C.c_int, _dp, C.c_void_p]),
     ("dc_gb300_source", C.c_float, [C.c_float, C.c_int, C.c_double]),
@@ -654,6 +674,100 @@ class Batch:
     @property
     def points(self) -> int:
         return int(lib().dc_gb300_batch_points(self.h))
+
+
+MLP_PARAMS = 32 * 32 + 16 * 32 + 32 * 32 + 32 + 2 * 32 + 2
+MLP_DEPTHS = 16
+SAMPLE_STRIDE = 33
+
+
+class MLP:
+    """The learned layer's network (dc_gb300_mlp_*).  Sample and target
+    arrays are device pointers (ints), e.g. torch tensors' data_ptr()."""
+
+    def __init__(self, device=-1, seed=None, params=None):
+        h = C.c_void_p()
+        check(lib().dc_gb300_mlp_create(int(device), C.byref(h)))
+        self.h = h.value
+        if params is not None:
+            self.set_params(params)
+        elif seed is not None:
+            check(lib().dc_gb300_mlp_init(self.h, int(seed)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().dc_gb300_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_params(self, params) -> None:
+        a = _f32(params).reshape(-1)
+        if a.size != MLP_PARAMS:
+            raise ValueError(f"expected {MLP_PARAMS} parameters")
+        check(lib().dc_gb300_mlp_set_params(self.h, fptr(a)))
+
+    def params(self) -> np.ndarray:
+        out = np.empty(MLP_PARAMS, np.float32)
+        check(lib().dc_gb300_mlp_get_params(self.h, fptr(out)))
+        return out
+
+    def forward(self, samples_ptr: int, n: int, out_ptr: int) -> None:
+        check(lib().dc_gb300_mlp_forward(self.h, samples_ptr, int(n), out_ptr))
+
+    def gradient(self, samples_ptr: int, targets_ptr: int, n: int):
+        g = np.empty(MLP_PARAMS, np.float32)
+        loss = (C.c_double * 2)()
+        check(lib().dc_gb300_mlp_gradient(self.h, samples_ptr, targets_ptr, int(n), fptr(g), loss))
+        return g, (loss[0], loss[1])
+
+    def train(self, samples_ptr: int, targets_ptr: int, n: int, steps: int, batch: int,
+              lr: float, seed: int = 0) -> np.ndarray:
+        hist = np.empty(max(1, steps), np.float32)
+        check(lib().dc_gb300_mlp_train(self.h, samples_ptr, targets_ptr, int(n), int(steps),
+                                       int(batch), float(lr), int(seed), fptr(hist)))
+        return hist[:steps]
+
+
+def layer_cells(sizes, layer: int) -> np.ndarray:
+    """[n][4] table (x, y, z, axis | side << 2 | depth << 3) of the layer cells."""
+    n = lib().dc_gb300_layer_cells(*[int(v) for v in sizes], int(layer), None, 0)
+    if n < 0:
+        raise DcError(ERR_ARG, last_error())
+    out = np.empty((n, 4), np.int32)
+    lib().dc_gb300_layer_cells(*[int(v) for v in sizes], int(layer),
+                               out.ctypes.data_as(C.POINTER(C.c_int)), n)
+    return out
+
+
+def set_learned_layer(sim: "Simulation", mlp: "MLP | None", layer: int) -> None:
+    check(lib().dc_gb300_set_learned_layer(sim.h, mlp.h if mlp is not None else None, int(layer)))
+
+
+def lb_sample(wide: "Simulation", thin: "Simulation", offset, layer: int, samples_ptr: int,
+              targets_ptr: int, cap: int) -> int:
+    n = C.c_longlong()
+    check(lib().dc_gb300_lb_sample(wide.h, thin.h, (C.c_long * 3)(*[int(v) for v in offset]),
+                                   int(layer), samples_ptr, targets_ptr, int(cap), C.byref(n)))
+    return n.value
+
+
+def lb_rollout(wide: "Simulation", thin: "Simulation", offset, steps: int, samples_ptr: int,
+               targets_ptr: int, cap: int) -> int:
+    n = C.c_longlong()
+    check(lib().dc_gb300_lb_rollout(wide.h, thin.h, (C.c_long * 3)(*[int(v) for v in offset]),
+                                    int(steps), samples_ptr, targets_ptr, int(cap), C.byref(n)))
+    return n.value
 
 
 def header_symbols() -> list[str]:

@@ -7,6 +7,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "dc_gb300.h"
 
@@ -163,6 +164,13 @@ struct Sim {
   // tensor maps for the fast kernel (encoded for one tile shape)
   CUtensorMap tm_halo[2], tm_own[2], tm_c[3];
   int maps_tx = 0, maps_ty = 0;
+  // learned absorbing layer, applied after every stencil pass of a run
+  const float *lb_params = nullptr;  // MLP compute parameters (device, owned by the MLP)
+  int4 *d_lb_cells = nullptr;        // layer-cell table
+  float2 *d_lb_corr = nullptr;       // corrections of one step
+  long long lb_cells = 0;
+  int lb_layer = 0;
+  float *lb_rec = nullptr;           // rollout training: record the step's samples here
   // captured multi-step graphs, keyed by start parity of the pc buffer
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   int graph_steps[2] = {0, 0};
@@ -258,6 +266,30 @@ bool encode_tiled(CUtensorMap *map, const void *base, int rank,
                   const uint64_t *dims, const uint64_t *strides_bytes,
                   const uint32_t *box, std::string *err,
                   CUtensorMapDataType type = CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
+
+// Learned absorbing layer (dc_learned.cu).  Layer cells of a box with a
+// layer of `layer` cells: {x, y, z, axis | side << 2 | depth << 3}.
+std::vector<int4> layer_cells(long long sx, long long sy, long long sz, int layer);
+// Corrections of every layer cell from the new (t+1) and current (t)
+// fields, then added to the new field.
+// `rec` (may be null) also receives every cell's features (sample rows).
+cudaError_t launch_lb_step(cudaStream_t st, const float *params, const int4 *cells, long long n,
+                           float2 *nw, const float2 *cur, long long pitch, long long plane,
+                           float2 *corr, float *rec);
+// Rollout targets from recorded rows: wide (at `off`) minus features 0 / 8.
+cudaError_t launch_lb_target(cudaStream_t st, const int4 *cells, long long n, const float *rows,
+                             const float2 *wide, long long wpitch, long long wplane,
+                             const int off[3], float *ts);
+// Training samples ([n][33] features + depth, [n][2] targets) of a thin box
+// stepped from a crop of a wide box at `off`.
+cudaError_t launch_lb_sample(cudaStream_t st, const int4 *cells, long long n, const float2 *nw,
+                             const float2 *cur, long long pitch, long long plane,
+                             const float2 *wide, long long wpitch, long long wplane,
+                             const int off[3], float *xs, float *ts);
+// Thin pair buffer <- box of a wide pair buffer at `off`, zero halo.
+cudaError_t launch_crop(cudaStream_t st, float2 *dst, long long sx, long long sy, long long sz,
+                        long long pitch, const float2 *src, long long wpitch, long long wplane,
+                        const int off[3]);
 
 // FD weights, inverse spacings, dt and dt^2 of a pass (the vexp scaling of
 // the narrow medium forms is applied by the caller).

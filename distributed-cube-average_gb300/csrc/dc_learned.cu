@@ -1,0 +1,777 @@
+// dc_learned.cu -- the learned thin absorbing layer.
+//
+// A thin layer of L cells (L <= DC_GB300_MLP_DEPTHS) between the physical
+// interior and the 4-cell halo replaces the wide sponge.  After every
+// stencil pass, each of the layer's 4 outer cells -- those whose stencils
+// reach into the zero halo -- gets a correction (dp, dq) predicted by a
+// small MLP from the cells along its boundary normal (the inner L - 4 cells
+// are updated by the stencil alone):
+//
+//   features  the cell and the 7 cells inward along the normal, p and q, at
+//             t+1 (the stencil's output) and t: 8 x 2 x 2 = 32 values
+//   scale     r = rms of the 32 features; the network sees x / r and its
+//             output is multiplied by r (the correction is homogeneous of
+//             degree 1 in the wavefield, like a linear absorbing condition)
+//   network   32 -> 32 -> 32 -> 2, GELU, BF16 weights and activations, FP32
+//             accumulation; the first hidden layer's bias depends on the
+//             cell's depth in the layer (0 = next to the interior)
+//
+// The normal of an edge or corner cell is the axis along which it lies
+// deepest in the layer (lowest axis on ties).
+//
+// Training (teacher forcing): a wide simulation, whose margins keep every
+// reflection out of the region of interest for the whole run, supplies the
+// truth.  At a sampled step its fields (t and t-1) are cropped to the thin
+// box (zero halo), stepped once by the thin simulation, and every layer cell
+// yields a sample (features of the thin step) and a target (wide field at
+// t+1 minus the thin step).  The loss is sum |r * y - target|^2 / sum r^2
+// over a minibatch; gradients run through the BF16 roundings unchanged;
+// Adam updates FP32 master weights.  Every kernel here is this project's own.
+//
+// The reference has no learned boundary; it absorbs with its random
+// velocity boundary (src/boundary.c:7-104).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "dc_internal.h"
+
+namespace dcg {
+namespace {
+
+constexpr int kIn = DC_GB300_MLP_IN, kHid = DC_GB300_MLP_HIDDEN, kOut = DC_GB300_MLP_OUT;
+constexpr int kDepths = DC_GB300_MLP_DEPTHS;
+constexpr int kStride = kIn + 1;  // sample row: 32 features + depth
+constexpr int OFF_W1 = 0;                         // [kHid][kIn]
+constexpr int OFF_B1 = OFF_W1 + kHid * kIn;       // [kDepths][kHid]
+constexpr int OFF_W2 = OFF_B1 + kDepths * kHid;   // [kHid][kHid]
+constexpr int OFF_B2 = OFF_W2 + kHid * kHid;      // [kHid]
+constexpr int OFF_W3 = OFF_B2 + kHid;             // [kOut][kHid]
+constexpr int OFF_B3 = OFF_W3 + kOut * kHid;      // [kOut]
+constexpr int kParams = OFF_B3 + kOut;
+static_assert(kParams == DC_GB300_MLP_PARAMS, "parameter count");
+constexpr int kWin = 8;  // cells along the normal
+
+__device__ __forceinline__ bool is_weight(int p) {
+  return (p >= OFF_W1 && p < OFF_B1) || (p >= OFF_W2 && p < OFF_B2) || (p >= OFF_W3 && p < OFF_B3);
+}
+
+__device__ __forceinline__ float bf16r(float v) {
+  return __bfloat162float(__float2bfloat16_rn(v));
+}
+
+__device__ __forceinline__ float gelu(float a) {
+  return 0.5f * a * (1.0f + erff(a * 0.70710678118654752f));
+}
+
+__device__ __forceinline__ float gelu_grad(float a) {
+  const float cdf = 0.5f * (1.0f + erff(a * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * a * a);
+  return cdf + a * pdf;
+}
+
+// Copies the compute parameters into shared memory.
+__device__ __forceinline__ void load_params(float *sw, const float *wc) {
+  for (int i = threadIdx.x; i < kParams; i += blockDim.x) sw[i] = wc[i];
+}
+
+// Forward pass of one sample from raw features x[32] (r = rms, 0 if
+// silent); writes y[2] (network output before the r scaling).
+__device__ __forceinline__ float forward(const float *sw, const float *x, int depth, float y[kOut]) {
+  float ss = 0.0f;
+#pragma unroll
+  for (int k = 0; k < kIn; ++k) ss = fmaf(x[k], x[k], ss);
+  const float r = sqrtf(ss * (1.0f / kIn));
+  if (!(r > 0.0f)) {
+    y[0] = y[1] = 0.0f;
+    return 0.0f;
+  }
+  const float inv = 1.0f / r;
+  float xh[kIn];
+#pragma unroll
+  for (int k = 0; k < kIn; ++k) xh[k] = bf16r(x[k] * inv);
+  float h1[kHid];
+  const float *b1 = sw + OFF_B1 + depth * kHid;
+#pragma unroll 4
+  for (int o = 0; o < kHid; ++o) {
+    float a = b1[o];
+    const float *w = sw + OFF_W1 + o * kIn;
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) a = fmaf(w[k], xh[k], a);
+    h1[o] = bf16r(gelu(a));
+  }
+  float h2[kHid];
+#pragma unroll 4
+  for (int o = 0; o < kHid; ++o) {
+    float a = sw[OFF_B2 + o];
+    const float *w = sw + OFF_W2 + o * kHid;
+#pragma unroll
+    for (int k = 0; k < kHid; ++k) a = fmaf(w[k], h1[k], a);
+    h2[o] = bf16r(gelu(a));
+  }
+#pragma unroll
+  for (int j = 0; j < kOut; ++j) {
+    float a = sw[OFF_B3 + j];
+    const float *w = sw + OFF_W3 + j * kHid;
+#pragma unroll
+    for (int k = 0; k < kHid; ++k) a = fmaf(w[k], h2[k], a);
+    y[j] = a;
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Training: gradient of sum_i |r_i y_i - t_i|^2 over a set of samples.
+// 128 samples per CTA pass; per-sample activations and deltas live in
+// shared memory so the weight gradients are small block GEMMs over the
+// 128 samples.  `sampled` = 0: samples [0, count); 1: `count` samples
+// drawn with replacement from [0, n) by hashing `seed`.
+constexpr int kTB = 128;
+constexpr int kRow = 33;  // padded row (no bank conflicts)
+constexpr int SM_W = 0;
+constexpr int SM_XH = SM_W + kParams;
+constexpr int SM_A1 = SM_XH + kTB * kRow;   // a1, then delta1
+constexpr int SM_H1 = SM_A1 + kTB * kRow;
+constexpr int SM_A2 = SM_H1 + kTB * kRow;   // a2, then delta2
+constexpr int SM_H2 = SM_A2 + kTB * kRow;
+constexpr int SM_DY = SM_H2 + kTB * kRow;   // [kTB][2]
+constexpr int SM_DEP = SM_DY + kTB * 2;     // int
+constexpr int SM_FLOATS = SM_DEP + kTB;
+constexpr size_t kGradSmem = sizeof(float) * SM_FLOATS;
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(kTB) mlp_grad_kernel(const float *__restrict__ wc,
+                                                       const float *__restrict__ xs,
+                                                       const float *__restrict__ ts, long long n,
+                                                       long long count, unsigned long long seed,
+                                                       int sampled, float *grad, double *acc) {
+  extern __shared__ float sm[];
+  float *sw = sm + SM_W;
+  float *XH = sm + SM_XH, *A1 = sm + SM_A1, *H1 = sm + SM_H1, *A2 = sm + SM_A2, *H2 = sm + SM_H2;
+  float *DY = sm + SM_DY;
+  int *DEP = reinterpret_cast<int *>(sm + SM_DEP);
+  load_params(sw, wc);
+  const int t = threadIdx.x;
+  // per-thread gradient accumulators: W1 (8), W2 (8), b1 (kDepths*kHid/128),
+  // W3 / b2 / b3 (first threads)
+  float gW1[8], gW2[8], gB1[kDepths * kHid / kTB];
+  float gW3 = 0.f, gB2 = 0.f, gB3 = 0.f;
+#pragma unroll
+  for (int m = 0; m < 8; ++m) gW1[m] = gW2[m] = 0.f;
+#pragma unroll
+  for (int m = 0; m < kDepths * kHid / kTB; ++m) gB1[m] = 0.f;
+  double l_err = 0.0, l_w = 0.0;
+  __syncthreads();
+  for (long long base = static_cast<long long>(blockIdx.x) * kTB; base < count;
+       base += static_cast<long long>(gridDim.x) * kTB) {
+    const long long j = base + t;
+    bool live = j < count;
+    long long i = j;
+    if (live && sampled) i = static_cast<long long>(mix64(seed ^ (static_cast<unsigned long long>(j) * 0x2545F4914F6CDD1Dull)) % static_cast<unsigned long long>(n));
+    float x[kIn];
+    int depth = 0;
+    float r = 0.f;
+    if (live) {
+      const float *row = xs + i * kStride;
+#pragma unroll
+      for (int k = 0; k < kIn; ++k) x[k] = row[k];
+      depth = min(max(static_cast<int>(row[kIn]), 0), kDepths - 1);
+      float ss = 0.f;
+#pragma unroll
+      for (int k = 0; k < kIn; ++k) ss = fmaf(x[k], x[k], ss);
+      r = sqrtf(ss * (1.0f / kIn));
+      live = r > 0.f;
+    }
+    float *xh = XH + t * kRow, *a1 = A1 + t * kRow, *h1 = H1 + t * kRow;
+    float *a2 = A2 + t * kRow, *h2 = H2 + t * kRow;
+    DEP[t] = depth;
+    if (!live) {
+      for (int k = 0; k < kRow; ++k) xh[k] = a1[k] = h1[k] = a2[k] = h2[k] = 0.f;
+      DY[2 * t] = DY[2 * t + 1] = 0.f;
+    } else {
+      const float inv = 1.0f / r;
+      for (int k = 0; k < kIn; ++k) xh[k] = bf16r(x[k] * inv);
+      for (int o = 0; o < kHid; ++o) {
+        float a = sw[OFF_B1 + depth * kHid + o];
+        const float *w = sw + OFF_W1 + o * kIn;
+        for (int k = 0; k < kIn; ++k) a = fmaf(w[k], xh[k], a);
+        a1[o] = a;
+        h1[o] = bf16r(gelu(a));
+      }
+      for (int o = 0; o < kHid; ++o) {
+        float a = sw[OFF_B2 + o];
+        const float *w = sw + OFF_W2 + o * kHid;
+        for (int k = 0; k < kHid; ++k) a = fmaf(w[k], h1[k], a);
+        a2[o] = a;
+        h2[o] = bf16r(gelu(a));
+      }
+      float dy[kOut];
+      for (int jj = 0; jj < kOut; ++jj) {
+        float a = sw[OFF_B3 + jj];
+        const float *w = sw + OFF_W3 + jj * kHid;
+        for (int k = 0; k < kHid; ++k) a = fmaf(w[k], h2[k], a);
+        const float e = r * a - ts[i * kOut + jj];
+        l_err += static_cast<double>(e) * e;
+        dy[jj] = 2.0f * r * e;
+        DY[2 * t + jj] = dy[jj];
+      }
+      l_w += static_cast<double>(r) * r;
+      // delta2 = (W3^T dy) * gelu'(a2), stored over a2
+      for (int o = 0; o < kHid; ++o) {
+        float d = 0.f;
+        for (int jj = 0; jj < kOut; ++jj) d = fmaf(sw[OFF_W3 + jj * kHid + o], dy[jj], d);
+        a2[o] = d * gelu_grad(a2[o]);
+      }
+      // delta1 = (W2^T delta2) * gelu'(a1), stored over a1
+      for (int k = 0; k < kHid; ++k) {
+        float d = 0.f;
+        for (int o = 0; o < kHid; ++o) d = fmaf(sw[OFF_W2 + o * kHid + k], a2[o], d);
+        a1[k] = d * gelu_grad(a1[k]);
+      }
+    }
+    __syncthreads();
+    // weight gradients: sums over the 128 samples of this pass
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int e = t + kTB * m, o = e >> 5, k = e & 31;
+      float s1 = 0.f, s2 = 0.f;
+      for (int s = 0; s < kTB; ++s) {
+        s1 = fmaf(A1[s * kRow + o], XH[s * kRow + k], s1);
+        s2 = fmaf(A2[s * kRow + o], H1[s * kRow + k], s2);
+      }
+      gW1[m] += s1;
+      gW2[m] += s2;
+    }
+#pragma unroll
+    for (int m = 0; m < kDepths * kHid / kTB; ++m) {
+      const int e = t + kTB * m, dd = e / kHid, o = e % kHid;
+      float s1 = 0.f;
+      for (int s = 0; s < kTB; ++s)
+        if (DEP[s] == dd) s1 += A1[s * kRow + o];
+      gB1[m] += s1;
+    }
+    if (t < kOut * kHid) {
+      const int jj = t / kHid, o = t % kHid;
+      float s3 = 0.f;
+      for (int s = 0; s < kTB; ++s) s3 = fmaf(DY[2 * s + jj], H2[s * kRow + o], s3);
+      gW3 += s3;
+    }
+    if (t < kHid) {
+      float s2 = 0.f;
+      for (int s = 0; s < kTB; ++s) s2 += A2[s * kRow + t];
+      gB2 += s2;
+    }
+    if (t < kOut) {
+      float s3 = 0.f;
+      for (int s = 0; s < kTB; ++s) s3 += DY[2 * s + t];
+      gB3 += s3;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    atomicAdd(&grad[OFF_W1 + t + kTB * m], gW1[m]);
+    atomicAdd(&grad[OFF_W2 + t + kTB * m], gW2[m]);
+  }
+#pragma unroll
+  for (int m = 0; m < kDepths * kHid / kTB; ++m) atomicAdd(&grad[OFF_B1 + t + kTB * m], gB1[m]);
+  if (t < kOut * kHid) atomicAdd(&grad[OFF_W3 + t], gW3);
+  if (t < kHid) atomicAdd(&grad[OFF_B2 + t], gB2);
+  if (t < kOut) atomicAdd(&grad[OFF_B3 + t], gB3);
+  // loss sums
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    l_err += __shfl_down_sync(0xffffffffu, l_err, off);
+    l_w += __shfl_down_sync(0xffffffffu, l_w, off);
+  }
+  if ((t & 31) == 0) {
+    atomicAdd(&acc[0], l_err);
+    atomicAdd(&acc[1], l_w);
+  }
+}
+
+// Adam step on the FP32 master weights with the gradient of the mean loss
+// (grad / sum r^2); refreshes the compute copy (weights rounded to BF16),
+// clears the gradient and the loss sums, and records the loss.
+__global__ void mlp_adam_kernel(float *master, float *wc, float *m1, float *m2, float *grad,
+                                double *acc, float lr, float b1, float b2, float eps, int step,
+                                float *loss_hist, int hist_index) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const double w = acc[1];
+  if (p < kParams) {
+    const float g = w > 0.0 ? static_cast<float>(grad[p] / w) : 0.0f;
+    const float a = b1 * m1[p] + (1.0f - b1) * g;
+    const float v = b2 * m2[p] + (1.0f - b2) * g * g;
+    m1[p] = a;
+    m2[p] = v;
+    const float ah = a / (1.0f - powf(b1, static_cast<float>(step)));
+    const float vh = v / (1.0f - powf(b2, static_cast<float>(step)));
+    const float nw = master[p] - lr * ah / (sqrtf(vh) + eps);
+    master[p] = nw;
+    wc[p] = is_weight(p) ? bf16r(nw) : nw;
+    grad[p] = 0.0f;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0 && loss_hist)
+    loss_hist[hist_index] = w > 0.0 ? static_cast<float>(acc[0] / w) : 0.0f;
+}
+
+__global__ void mlp_clear_acc_kernel(double *acc) {
+  if (threadIdx.x < 2) acc[threadIdx.x] = 0.0;
+}
+
+// Compute copy of a parameter vector.
+__global__ void mlp_round_kernel(const float *master, float *wc) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < kParams) wc[p] = is_weight(p) ? bf16r(master[p]) : master[p];
+}
+
+// Network output (r * y: the correction) for n samples.
+__global__ void __launch_bounds__(128) mlp_forward_kernel(const float *__restrict__ wc,
+                                                          const float *__restrict__ xs,
+                                                          long long n, float *out) {
+  __shared__ float sw[kParams];
+  load_params(sw, wc);
+  __syncthreads();
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    float x[kIn];
+    const float *row = xs + i * kStride;
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) x[k] = row[k];
+    const int depth = min(max(static_cast<int>(row[kIn]), 0), kDepths - 1);
+    float y[kOut];
+    const float r = forward(sw, x, depth, y);
+    out[i * kOut] = r * y[0];
+    out[i * kOut + 1] = r * y[1];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Layer cells: int4 {x, y, z, meta}, meta = axis | side << 2 | depth << 3
+// (side 1 = the high end of the axis).
+
+// The 32 features of cell c from the new (t+1) and current (t) pair
+// buffers; returns the depth.
+__device__ __forceinline__ int gather(const int4 c, const float2 *nw, const float2 *cur,
+                                      long long pitch, long long plane, float x[kIn]) {
+  const int axis = c.w & 3, side = (c.w >> 2) & 1, depth = c.w >> 3;
+  const long long stride = axis == 0 ? 1 : axis == 1 ? pitch : plane;
+  const long long step = side ? -stride : stride;  // inward
+  long long g = static_cast<long long>(c.z) * plane + static_cast<long long>(c.y) * pitch + c.x;
+#pragma unroll
+  for (int k = 0; k < kWin; ++k) {
+    const float2 a = nw[g], b = cur[g];
+    x[k] = a.x;
+    x[kWin + k] = a.y;
+    x[2 * kWin + k] = b.x;
+    x[3 * kWin + k] = b.y;
+    g += step;
+  }
+  return depth;
+}
+
+// `rec` (may be null): the features and depth of every cell are also
+// written there as sample rows (rollout training).
+__global__ void __launch_bounds__(128) lb_infer_kernel(const float *__restrict__ wc,
+                                                       const int4 *__restrict__ cells,
+                                                       long long n, const float2 *nw,
+                                                       const float2 *cur, long long pitch,
+                                                       long long plane, float2 *corr,
+                                                       float *rec) {
+  __shared__ float sw[kParams];
+  load_params(sw, wc);
+  __syncthreads();
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    float x[kIn];
+    const int depth = gather(cells[i], nw, cur, pitch, plane, x);
+    if (rec) {
+      float *row = rec + i * kStride;
+#pragma unroll
+      for (int k = 0; k < kIn; ++k) row[k] = x[k];
+      row[kIn] = static_cast<float>(depth);
+    }
+    float y[kOut];
+    const float r = forward(sw, x, depth, y);
+    corr[i] = make_float2(r * y[0], r * y[1]);
+  }
+}
+
+__global__ void lb_add_kernel(const int4 *__restrict__ cells, long long n, float2 *nw,
+                              const float2 *__restrict__ corr, long long pitch, long long plane) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int4 c = cells[i];
+    const long long g = static_cast<long long>(c.z) * plane + static_cast<long long>(c.y) * pitch + c.x;
+    const float2 d = corr[i], v = nw[g];
+    nw[g] = make_float2(v.x + d.x, v.y + d.y);
+  }
+}
+
+// Training samples of the thin box: features from its step and targets
+// from the wide field (offset into the wide box).
+__global__ void lb_sample_kernel(const int4 *__restrict__ cells, long long n, const float2 *nw,
+                                 const float2 *cur, long long pitch, long long plane,
+                                 const float2 *wide, long long wpitch, long long wplane, int ox,
+                                 int oy, int oz, float *xs, float *ts) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int4 c = cells[i];
+    float x[kIn];
+    const int depth = gather(c, nw, cur, pitch, plane, x);
+    float *row = xs + i * kStride;
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) row[k] = x[k];
+    row[kIn] = static_cast<float>(depth);
+    const long long g = static_cast<long long>(c.z) * plane + static_cast<long long>(c.y) * pitch + c.x;
+    const long long w = static_cast<long long>(c.z + oz) * wplane +
+                        static_cast<long long>(c.y + oy) * wpitch + (c.x + ox);
+    const float2 tv = wide[w], sv = nw[g];
+    ts[i * kOut] = tv.x - sv.x;
+    ts[i * kOut + 1] = tv.y - sv.y;
+  }
+}
+
+// Rollout targets: wide field at t+1 minus the thin stencil's output, which
+// is features 0 (p) and 8 (q) of each recorded row.
+__global__ void lb_target_kernel(const int4 *__restrict__ cells, long long n,
+                                 const float *__restrict__ rows, const float2 *wide,
+                                 long long wpitch, long long wplane, int ox, int oy, int oz,
+                                 float *ts) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int4 c = cells[i];
+    const long long w = static_cast<long long>(c.z + oz) * wplane +
+                        static_cast<long long>(c.y + oy) * wpitch + (c.x + ox);
+    const float2 tv = wide[w];
+    ts[i * kOut] = tv.x - rows[i * kStride];
+    ts[i * kOut + 1] = tv.y - rows[i * kStride + kWin];
+  }
+}
+
+// Thin box <- wide box at (ox, oy, oz), zero outside [4, s-4)^3.
+__global__ void crop_kernel(float2 *dst, long long sx, long long sy, long long sz,
+                            long long pitch, const float2 *src, long long wpitch,
+                            long long wplane, int ox, int oy, int oz) {
+  const long long n = sx * sy * sz;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long x = i % sx, y = (i / sx) % sy, z = i / (sx * sy);
+    float2 v = make_float2(0.f, 0.f);
+    if (x >= 4 && x < sx - 4 && y >= 4 && y < sy - 4 && z >= 4 && z < sz - 4)
+      v = src[(z + oz) * wplane + (y + oy) * wpitch + (x + ox)];
+    dst[(z * sy + y) * pitch + x] = v;
+  }
+}
+
+int grid_for(long long n, int per_block) {
+  return static_cast<int>(std::max<long long>(1, std::min<long long>((n + per_block - 1) / per_block, 152 * 16)));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+constexpr int kCorrected = 4;  // outer layer cells corrected by the network
+
+std::vector<int4> layer_cells(long long sx, long long sy, long long sz, int layer) {
+  std::vector<int4> out;
+  const long long s[3] = {sx, sy, sz};
+  auto depth_on = [&](int a, long long c, int *side) -> int {
+    const long long lo = 4 + layer, hi = s[a] - 4 - layer;
+    if (c < lo) {
+      *side = 0;
+      return static_cast<int>(lo - 1 - c);
+    }
+    if (c >= hi) {
+      *side = 1;
+      return static_cast<int>(c - hi);
+    }
+    return -1;
+  };
+  for (long long z = 4; z < sz - 4; ++z)
+    for (long long y = 4; y < sy - 4; ++y) {
+      int sdz = 0, sdy = 0;
+      const int dz = depth_on(2, z, &sdz), dy = depth_on(1, y, &sdy);
+      const bool band = dz < 0 && dy < 0;  // only the two x slabs are in the layer
+      for (long long x = 4; x < sx - 4; ++x) {
+        if (band && x == 4 + layer) x = sx - 4 - layer;  // skip the interior
+        int sdx = 0;
+        const int dx = depth_on(0, x, &sdx);
+        int axis = -1, depth = -1, side = 0;
+        if (dx > depth) { axis = 0; depth = dx; side = sdx; }
+        if (dy > depth) { axis = 1; depth = dy; side = sdy; }
+        if (dz > depth) { axis = 2; depth = dz; side = sdz; }
+        // only the outer cells, whose stencils reach into the halo, are
+        // corrected; the inner ones are updated by the stencil alone
+        if (axis < 0 || depth < layer - kCorrected) continue;
+        out.push_back(make_int4(static_cast<int>(x), static_cast<int>(y), static_cast<int>(z),
+                                axis | side << 2 | depth << 3));
+      }
+    }
+  return out;
+}
+
+cudaError_t launch_lb_step(cudaStream_t st, const float *wc, const int4 *cells, long long n,
+                           float2 *nw, const float2 *cur, long long pitch, long long plane,
+                           float2 *corr, float *rec) {
+  lb_infer_kernel<<<grid_for(n, 128), 128, 0, st>>>(wc, cells, n, nw, cur, pitch, plane, corr,
+                                                    rec);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  lb_add_kernel<<<grid_for(n, 256), 256, 0, st>>>(cells, n, nw, corr, pitch, plane);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lb_sample(cudaStream_t st, const int4 *cells, long long n, const float2 *nw,
+                             const float2 *cur, long long pitch, long long plane,
+                             const float2 *wide, long long wpitch, long long wplane,
+                             const int off[3], float *xs, float *ts) {
+  lb_sample_kernel<<<grid_for(n, 256), 256, 0, st>>>(cells, n, nw, cur, pitch, plane, wide,
+                                                     wpitch, wplane, off[0], off[1], off[2], xs,
+                                                     ts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lb_target(cudaStream_t st, const int4 *cells, long long n, const float *rows,
+                             const float2 *wide, long long wpitch, long long wplane,
+                             const int off[3], float *ts) {
+  lb_target_kernel<<<grid_for(n, 256), 256, 0, st>>>(cells, n, rows, wide, wpitch, wplane,
+                                                     off[0], off[1], off[2], ts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_crop(cudaStream_t st, float2 *dst, long long sx, long long sy, long long sz,
+                        long long pitch, const float2 *src, long long wpitch, long long wplane,
+                        const int off[3]) {
+  crop_kernel<<<grid_for(sx * sy * sz, 256), 256, 0, st>>>(dst, sx, sy, sz, pitch, src, wpitch,
+                                                           wplane, off[0], off[1], off[2]);
+  return cudaGetLastError();
+}
+
+}  // namespace dcg
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+struct dc_gb300_mlp {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  float *master = nullptr, *wc = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr;
+  double *acc = nullptr;
+  int adam_step = 0;
+};
+
+namespace {
+
+int fail(int code, const std::string &msg) {
+  dcg::set_error(msg);
+  return code;
+}
+
+#define LB_TRY(call)                                                                 \
+  do {                                                                               \
+    const cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess)                                                           \
+      return fail(DC_GB300_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+void release(dc_gb300_mlp *m) {
+  cudaFree(m->master);
+  cudaFree(m->wc);
+  cudaFree(m->m1);
+  cudaFree(m->m2);
+  cudaFree(m->grad);
+  cudaFree(m->acc);
+  if (m->stream) cudaStreamDestroy(m->stream);
+}
+
+}  // namespace
+
+extern "C" int dc_gb300_mlp_create(int device, dc_gb300_mlp **out) {
+  if (!out) return fail(DC_GB300_ERR_ARG, "null argument");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(DC_GB300_ERR_DEVICE, "no CUDA device");
+  int dev = device;
+  if (dev < 0) LB_TRY(cudaGetDevice(&dev));
+  if (dev >= ndev) return fail(DC_GB300_ERR_DEVICE, "device ordinal out of range");
+  LB_TRY(cudaSetDevice(dev));
+  auto *m = new dc_gb300_mlp();
+  m->device = dev;
+  const size_t pb = sizeof(float) * dcg::kParams;
+  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&m->master, pb) != cudaSuccess || cudaMalloc(&m->wc, pb) != cudaSuccess ||
+      cudaMalloc(&m->m1, pb) != cudaSuccess || cudaMalloc(&m->m2, pb) != cudaSuccess ||
+      cudaMalloc(&m->grad, pb) != cudaSuccess ||
+      cudaMalloc(&m->acc, 2 * sizeof(double)) != cudaSuccess) {
+    release(m);
+    delete m;
+    return fail(DC_GB300_ERR_NOMEM, "MLP buffers");
+  }
+  cudaMemsetAsync(m->master, 0, pb, m->stream);
+  cudaMemsetAsync(m->wc, 0, pb, m->stream);
+  cudaMemsetAsync(m->m1, 0, pb, m->stream);
+  cudaMemsetAsync(m->m2, 0, pb, m->stream);
+  cudaMemsetAsync(m->grad, 0, pb, m->stream);
+  cudaMemsetAsync(m->acc, 0, 2 * sizeof(double), m->stream);
+  if (cudaStreamSynchronize(m->stream) != cudaSuccess) {
+    release(m);
+    delete m;
+    return fail(DC_GB300_ERR_CUDA, "MLP set-up");
+  }
+  *out = m;
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_mlp_destroy(dc_gb300_mlp *m) {
+  if (!m) return DC_GB300_OK;
+  cudaSetDevice(m->device);
+  release(m);
+  delete m;
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_mlp_set_params(dc_gb300_mlp *m, const float *params) {
+  if (!m || !params) return fail(DC_GB300_ERR_ARG, "null argument");
+  LB_TRY(cudaSetDevice(m->device));
+  const size_t pb = sizeof(float) * dcg::kParams;
+  LB_TRY(cudaMemcpyAsync(m->master, params, pb, cudaMemcpyHostToDevice, m->stream));
+  dcg::mlp_round_kernel<<<(dcg::kParams + 255) / 256, 256, 0, m->stream>>>(m->master, m->wc);
+  LB_TRY(cudaGetLastError());
+  LB_TRY(cudaMemsetAsync(m->m1, 0, pb, m->stream));
+  LB_TRY(cudaMemsetAsync(m->m2, 0, pb, m->stream));
+  LB_TRY(cudaMemsetAsync(m->grad, 0, pb, m->stream));
+  LB_TRY(cudaStreamSynchronize(m->stream));
+  m->adam_step = 0;
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_mlp_init(dc_gb300_mlp *m, unsigned int seed) {
+  if (!m) return fail(DC_GB300_ERR_ARG, "null argument");
+  std::vector<float> p(dcg::kParams, 0.0f);
+  std::mt19937 rng(seed);
+  auto fill = [&](int off, int rows, int cols, float gain) {
+    const float sd = gain / std::sqrt(static_cast<float>(cols));
+    std::normal_distribution<float> nd(0.0f, sd);
+    for (int i = 0; i < rows * cols; ++i) p[off + i] = nd(rng);
+  };
+  fill(dcg::OFF_W1, dcg::kHid, dcg::kIn, 1.0f);
+  fill(dcg::OFF_W2, dcg::kHid, dcg::kHid, 1.0f);
+  fill(dcg::OFF_W3, dcg::kOut, dcg::kHid, 0.01f);  // corrections start near zero
+  return dc_gb300_mlp_set_params(m, p.data());
+}
+
+extern "C" int dc_gb300_mlp_get_params(dc_gb300_mlp *m, float *params) {
+  if (!m || !params) return fail(DC_GB300_ERR_ARG, "null argument");
+  LB_TRY(cudaSetDevice(m->device));
+  LB_TRY(cudaMemcpyAsync(params, m->master, sizeof(float) * dcg::kParams, cudaMemcpyDeviceToHost,
+                         m->stream));
+  LB_TRY(cudaStreamSynchronize(m->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_mlp_forward(dc_gb300_mlp *m, const float *samples, long long n,
+                                    float *out) {
+  if (!m || (n > 0 && (!samples || !out))) return fail(DC_GB300_ERR_ARG, "null argument");
+  if (n <= 0) return DC_GB300_OK;
+  LB_TRY(cudaSetDevice(m->device));
+  dcg::mlp_forward_kernel<<<dcg::grid_for(n, 128), 128, 0, m->stream>>>(m->wc, samples, n, out);
+  LB_TRY(cudaGetLastError());
+  LB_TRY(cudaStreamSynchronize(m->stream));
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_mlp_gradient(dc_gb300_mlp *m, const float *samples, const float *targets,
+                                     long long n, float *grad, double *loss) {
+  if (!m || !samples || !targets || !grad || n <= 0)
+    return fail(DC_GB300_ERR_ARG, "invalid argument");
+  LB_TRY(cudaSetDevice(m->device));
+  LB_TRY(cudaFuncSetAttribute(dcg::mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(dcg::kGradSmem)));
+  LB_TRY(cudaMemsetAsync(m->grad, 0, sizeof(float) * dcg::kParams, m->stream));
+  LB_TRY(cudaMemsetAsync(m->acc, 0, 2 * sizeof(double), m->stream));
+  dcg::mlp_grad_kernel<<<dcg::grid_for(n, dcg::kTB), dcg::kTB, dcg::kGradSmem, m->stream>>>(
+      m->wc, samples, targets, n, n, 0ull, 0, m->grad, m->acc);
+  LB_TRY(cudaGetLastError());
+  double acc[2];
+  LB_TRY(cudaMemcpyAsync(grad, m->grad, sizeof(float) * dcg::kParams, cudaMemcpyDeviceToHost,
+                         m->stream));
+  LB_TRY(cudaMemcpyAsync(acc, m->acc, sizeof(acc), cudaMemcpyDeviceToHost, m->stream));
+  LB_TRY(cudaMemsetAsync(m->grad, 0, sizeof(float) * dcg::kParams, m->stream));
+  LB_TRY(cudaStreamSynchronize(m->stream));
+  if (loss) {
+    loss[0] = acc[0];
+    loss[1] = acc[1];
+  }
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_mlp_train(dc_gb300_mlp *m, const float *samples, const float *targets,
+                                  long long n, int steps, int batch, float lr,
+                                  unsigned long long seed, float *loss_hist) {
+  if (!m || !samples || !targets || n <= 0 || steps < 0 || batch < 1 || !(lr > 0))
+    return fail(DC_GB300_ERR_ARG, "invalid argument");
+  LB_TRY(cudaSetDevice(m->device));
+  LB_TRY(cudaFuncSetAttribute(dcg::mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(dcg::kGradSmem)));
+  float *d_hist = nullptr;
+  if (loss_hist && steps > 0) LB_TRY(cudaMalloc(&d_hist, sizeof(float) * steps));
+  LB_TRY(cudaMemsetAsync(m->grad, 0, sizeof(float) * dcg::kParams, m->stream));
+  dcg::mlp_clear_acc_kernel<<<1, 32, 0, m->stream>>>(m->acc);
+  cudaError_t e = cudaGetLastError();
+  const int blocks = dcg::grid_for(batch, dcg::kTB);
+  for (int s = 0; s < steps && e == cudaSuccess; ++s) {
+    dcg::mlp_grad_kernel<<<blocks, dcg::kTB, dcg::kGradSmem, m->stream>>>(
+        m->wc, samples, targets, n, batch, seed + 0x9E3779B97F4A7C15ull * (m->adam_step + 1), 1,
+        m->grad, m->acc);
+    ++m->adam_step;
+    dcg::mlp_adam_kernel<<<(dcg::kParams + 255) / 256, 256, 0, m->stream>>>(
+        m->master, m->wc, m->m1, m->m2, m->grad, m->acc, lr, 0.9f, 0.999f, 1e-8f, m->adam_step,
+        d_hist, s);
+    dcg::mlp_clear_acc_kernel<<<1, 32, 0, m->stream>>>(m->acc);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && d_hist)
+    e = cudaMemcpyAsync(loss_hist, d_hist, sizeof(float) * steps, cudaMemcpyDeviceToHost,
+                        m->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  cudaFree(d_hist);
+  if (e != cudaSuccess) return fail(DC_GB300_ERR_CUDA, std::string("MLP training: ") + cudaGetErrorString(e));
+  return DC_GB300_OK;
+}
+
+extern "C" long long dc_gb300_layer_cells(long sx, long sy, long sz, int layer, int *cells,
+                                         long long cap) {
+  if (layer < 1 || layer > DC_GB300_MLP_DEPTHS || sx < 2 * layer + 16 || sy < 2 * layer + 16 ||
+      sz < 2 * layer + 16) {
+    fail(DC_GB300_ERR_ARG, "invalid layer geometry");
+    return -1;
+  }
+  const std::vector<int4> v = dcg::layer_cells(sx, sy, sz, layer);
+  const long long n = static_cast<long long>(v.size());
+  if (cells)
+    for (long long i = 0; i < std::min(n, cap); ++i) {
+      cells[4 * i] = v[i].x;
+      cells[4 * i + 1] = v[i].y;
+      cells[4 * i + 2] = v[i].z;
+      cells[4 * i + 3] = v[i].w;
+    }
+  return n;
+}
+
+extern "C" const float *dc_gb300_mlp_device_params(const dc_gb300_mlp *m) {
+  return m ? m->wc : nullptr;
+}

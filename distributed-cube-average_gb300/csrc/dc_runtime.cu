@@ -137,6 +137,8 @@ void release(Sim *s) {
   cudaFree(s->d_energy);
   cudaFree(s->d_step);
   cudaFree(s->d_err);
+  cudaFree(s->d_lb_cells);
+  cudaFree(s->d_lb_corr);
   if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -251,6 +253,14 @@ cudaError_t queue_step(Sim *s, int j) {
   }
   cudaError_t e = launch_pass(s, p);
   if (e != cudaSuccess) return e;
+  if (s->lb_cells > 0) {  // learned layer: correct the new field's layer cells
+    int cur = -1, prev = -1;
+    roles(s, &cur, &prev);
+    s->launches += 2;
+    e = launch_lb_step(s->stream, s->lb_params, s->d_lb_cells, s->lb_cells, s->pq[prev],
+                       s->pq[cur], s->pitch, s->plane, s->d_lb_corr, s->lb_rec);
+    if (e != cudaSuccess) return e;
+  }
   swap_roles(&s->handle->abi);
   return cudaSuccess;
 }
@@ -903,6 +913,143 @@ extern "C" int dc_gb300_set_sponge(dc_gb300_sim *h, const float *gx, const float
   return DC_GB300_OK;
 }
 
+extern "C" int dc_gb300_set_learned_layer(dc_gb300_sim *h, const dc_gb300_mlp *mlp,
+                                          int layer) {
+  Sim *s = impl(h);
+  if (!s) return fail(DC_GB300_ERR_ARG, "null simulation");
+  if (layer < 0 || layer > DC_GB300_MLP_DEPTHS)
+    return fail(DC_GB300_ERR_ARG, "layer width must lie in [0, DC_GB300_MLP_DEPTHS]");
+  if (layer > 0 && !mlp) return fail(DC_GB300_ERR_ARG, "null MLP");
+  if (layer > 0 && (s->sx < 2 * layer + 16 || s->sy < 2 * layer + 16 || s->sz < 2 * layer + 16))
+    return fail(DC_GB300_ERR_ARG, "the interior must keep at least 8 cells per axis");
+  DCG_TRY(cudaSetDevice(s->device));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  drop_graphs(s);
+  ++s->config_version;
+  cudaFree(s->d_lb_cells);
+  cudaFree(s->d_lb_corr);
+  s->d_lb_cells = nullptr;
+  s->d_lb_corr = nullptr;
+  s->lb_cells = 0;
+  s->lb_layer = 0;
+  s->lb_params = nullptr;
+  if (layer == 0) return DC_GB300_OK;
+  const std::vector<int4> cells = layer_cells(s->sx, s->sy, s->sz, layer);
+  const long long n = static_cast<long long>(cells.size());
+  DCG_TRY(cudaMalloc(&s->d_lb_cells, sizeof(int4) * n));
+  DCG_TRY(cudaMalloc(&s->d_lb_corr, sizeof(float2) * n));
+  DCG_TRY(cudaMemcpyAsync(s->d_lb_cells, cells.data(), sizeof(int4) * n, cudaMemcpyHostToDevice,
+                          s->stream));
+  DCG_TRY(cudaStreamSynchronize(s->stream));
+  s->lb_cells = n;
+  s->lb_layer = layer;
+  s->lb_params = dc_gb300_mlp_device_params(mlp);
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_lb_sample(dc_gb300_sim *hw, dc_gb300_sim *ht, const long offset[3],
+                                  int layer, float *samples, float *targets, long long cap,
+                                  long long *count) {
+  Sim *w = impl(hw), *t = impl(ht);
+  if (!w || !t || !offset || !samples || !targets || !count)
+    return fail(DC_GB300_ERR_ARG, "null argument");
+  if (w->device != t->device) return fail(DC_GB300_ERR_ARG, "simulations on different devices");
+  if (layer < 1 || layer > DC_GB300_MLP_DEPTHS)
+    return fail(DC_GB300_ERR_ARG, "layer width must lie in [1, DC_GB300_MLP_DEPTHS]");
+  if (offset[0] < 0 || offset[1] < 0 || offset[2] < 0 || offset[0] + t->sx > w->sx ||
+      offset[1] + t->sy > w->sy || offset[2] + t->sz > w->sz)
+    return fail(DC_GB300_ERR_ARG, "the thin box must lie inside the wide box");
+  if (t->lb_cells > 0 || t->src_gi >= 0)
+    return fail(DC_GB300_ERR_STATE, "the thin simulation must have no learned layer or source");
+  DCG_TRY(cudaSetDevice(w->device));
+  const std::vector<int4> cells = layer_cells(t->sx, t->sy, t->sz, layer);
+  const long long n = static_cast<long long>(cells.size());
+  if (n > cap) return fail(DC_GB300_ERR_ARG, "sample capacity too small");
+  int wc = -1, wp = -1, tc = -1, tp = -1;
+  if (!roles(w, &wc, &wp) || !roles(t, &tc, &tp))
+    return fail(DC_GB300_ERR_STATE, "field pointers rearranged");
+  const int off[3] = {static_cast<int>(offset[0]), static_cast<int>(offset[1]),
+                      static_cast<int>(offset[2])};
+  // both simulations run on their own streams: order the work explicitly
+  DCG_TRY(cudaStreamSynchronize(w->stream));
+  DCG_TRY(cudaStreamSynchronize(t->stream));
+  // thin <- crop of the wide fields (as stored, i.e. with the wide source's
+  // pending injection, which the wide step consumes identically)
+  t->launches += 2;
+  DCG_TRY(launch_crop(t->stream, t->pq[tc], t->sx, t->sy, t->sz, t->pitch, w->pq[wc], w->pitch,
+                      w->plane, off));
+  DCG_TRY(launch_crop(t->stream, t->pq[tp], t->sx, t->sy, t->sz, t->pitch, w->pq[wp], w->pitch,
+                      w->plane, off));
+  int rc = dc_gb300_run(ht, 1);
+  if (rc != DC_GB300_OK) return rc;
+  rc = dc_gb300_run(hw, 1);
+  if (rc != DC_GB300_OK) return rc;
+  DCG_TRY(cudaStreamSynchronize(w->stream));
+  int4 *d_cells = nullptr;
+  DCG_TRY(cudaMalloc(&d_cells, sizeof(int4) * n));
+  cudaError_t e = cudaMemcpyAsync(d_cells, cells.data(), sizeof(int4) * n,
+                                  cudaMemcpyHostToDevice, t->stream);
+  // after the thin step: new field in buffer tp, time t in tc; wide t+1 in wp
+  if (e == cudaSuccess)
+    e = launch_lb_sample(t->stream, d_cells, n, t->pq[tp], t->pq[tc], t->pitch, t->plane,
+                         w->pq[wp], w->pitch, w->plane, off, samples, targets);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(t->stream);
+  cudaFree(d_cells);
+  if (e != cudaSuccess) return fail(DC_GB300_ERR_CUDA, std::string("lb_sample: ") + cudaGetErrorString(e));
+  ++t->launches;
+  *count = n;
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_lb_rollout(dc_gb300_sim *hw, dc_gb300_sim *ht, const long offset[3],
+                                   int steps, float *samples, float *targets, long long cap,
+                                   long long *count) {
+  Sim *w = impl(hw), *t = impl(ht);
+  if (!w || !t || !offset || !samples || !targets || !count)
+    return fail(DC_GB300_ERR_ARG, "null argument");
+  if (w->device != t->device) return fail(DC_GB300_ERR_ARG, "simulations on different devices");
+  if (t->lb_cells <= 0) return fail(DC_GB300_ERR_STATE, "the thin simulation has no learned layer");
+  if (t->src_gi >= 0) return fail(DC_GB300_ERR_STATE, "the thin simulation must have no source");
+  if (steps < 1) return fail(DC_GB300_ERR_ARG, "steps must be positive");
+  if (offset[0] < 0 || offset[1] < 0 || offset[2] < 0 || offset[0] + t->sx > w->sx ||
+      offset[1] + t->sy > w->sy || offset[2] + t->sz > w->sz)
+    return fail(DC_GB300_ERR_ARG, "the thin box must lie inside the wide box");
+  const long long n = t->lb_cells;
+  if (n * steps > cap) return fail(DC_GB300_ERR_ARG, "sample capacity too small");
+  DCG_TRY(cudaSetDevice(w->device));
+  int wc = -1, wp = -1, tc = -1, tp = -1;
+  if (!roles(w, &wc, &wp) || !roles(t, &tc, &tp))
+    return fail(DC_GB300_ERR_STATE, "field pointers rearranged");
+  const int off[3] = {static_cast<int>(offset[0]), static_cast<int>(offset[1]),
+                      static_cast<int>(offset[2])};
+  DCG_TRY(cudaStreamSynchronize(w->stream));
+  DCG_TRY(cudaStreamSynchronize(t->stream));
+  t->launches += 2;
+  DCG_TRY(launch_crop(t->stream, t->pq[tc], t->sx, t->sy, t->sz, t->pitch, w->pq[wc], w->pitch,
+                      w->plane, off));
+  DCG_TRY(launch_crop(t->stream, t->pq[tp], t->sx, t->sy, t->sz, t->pitch, w->pq[wp], w->pitch,
+                      w->plane, off));
+  int rc = DC_GB300_OK;
+  for (int j = 0; j < steps && rc == DC_GB300_OK; ++j) {
+    float *rows = samples + static_cast<long long>(j) * n * 33;
+    t->lb_rec = rows;
+    rc = dc_gb300_run(ht, 1);
+    t->lb_rec = nullptr;
+    if (rc != DC_GB300_OK) break;
+    DCG_TRY(cudaStreamSynchronize(t->stream));
+    rc = dc_gb300_run(hw, 1);
+    if (rc != DC_GB300_OK) break;
+    roles(w, &wc, &wp);  // the new wide field is now the current one
+    ++w->launches;
+    DCG_TRY(launch_lb_target(w->stream, t->d_lb_cells, n, rows, w->pq[wc], w->pitch, w->plane,
+                             off, targets + static_cast<long long>(j) * n * 2));
+    DCG_TRY(cudaStreamSynchronize(w->stream));
+  }
+  if (rc != DC_GB300_OK) return rc;
+  *count = n * steps;
+  return DC_GB300_OK;
+}
+
 extern "C" int dc_gb300_set_receivers(dc_gb300_sim *h, const long *index, int count,
                                       int max_steps) {
   Sim *s = impl(h);
@@ -1031,7 +1178,7 @@ int capture_chunk(Sim *s, cudaGraphExec_t *out) {
   return DC_GB300_OK;
 }
 
-long long launches_per_step(const Sim *) { return 1; }
+long long launches_per_step(const Sim *s) { return s->lb_cells > 0 ? 3 : 1; }
 
 }  // namespace
 

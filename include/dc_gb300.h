@@ -418,6 +418,77 @@ void *dc_gb300_batch_stream(dc_gb300_batch *batch);
 /* Updated points per step summed over the shots ((s-8) per axis). */
 long long dc_gb300_batch_points(const dc_gb300_batch *batch);
 
+/* ---- Part 4: the learned thin absorbing layer (no counterpart in the
+ * reference, which absorbs with its random velocity boundary,
+ * src/boundary.c:7-104) ----
+ *
+ * A layer of L cells between the interior and the 4-cell halo, corrected
+ * after every stencil pass by an MLP: for each layer cell, the cell and the
+ * 7 cells inward along its boundary normal, p and q at t+1 (the stencil's
+ * output) and t, are 32 features; r = their rms; the network maps x / r
+ * through 32 -> 32 -> 32 -> 2 (GELU; BF16 weights and activations, FP32
+ * accumulation; first-layer bias per depth in the layer) and r * output is
+ * added to the cell's (p, q).  Parameters (FP32, DC_GB300_MLP_PARAMS):
+ * W1[32][32] | b1[DEPTHS][32] | W2[32][32] | b2[32] | W3[2][32] | b3[2].
+ * Samples are rows of 33 floats (32 features, then the depth); targets rows
+ * of 2 floats. */
+#define DC_GB300_MLP_IN 32
+#define DC_GB300_MLP_HIDDEN 32
+#define DC_GB300_MLP_OUT 2
+#define DC_GB300_MLP_DEPTHS 16
+#define DC_GB300_MLP_PARAMS (32 * 32 + 16 * 32 + 32 * 32 + 32 + 2 * 32 + 2)
+
+typedef struct dc_gb300_mlp dc_gb300_mlp;
+
+int dc_gb300_mlp_create(int device, dc_gb300_mlp **out);
+int dc_gb300_mlp_destroy(dc_gb300_mlp *mlp);
+/* Seeded initialisation (normal, std 1/sqrt(fan-in); output layer x 0.01). */
+int dc_gb300_mlp_init(dc_gb300_mlp *mlp, unsigned int seed);
+int dc_gb300_mlp_set_params(dc_gb300_mlp *mlp, const float *params);
+int dc_gb300_mlp_get_params(dc_gb300_mlp *mlp, float *params);
+/* Device address of the parameters the kernels read (weights rounded to
+ * BF16); stable for the MLP's lifetime. */
+const float *dc_gb300_mlp_device_params(const dc_gb300_mlp *mlp);
+/* Corrections r * y for n device samples into device out[n][2]. */
+int dc_gb300_mlp_forward(dc_gb300_mlp *mlp, const float *samples, long long n, float *out);
+/* Gradient (host grad[DC_GB300_MLP_PARAMS]) of sum |r*y - target|^2 over
+ * the n device samples; loss[0] = that sum, loss[1] = sum r^2. */
+int dc_gb300_mlp_gradient(dc_gb300_mlp *mlp, const float *samples, const float *targets,
+                          long long n, float *grad, double *loss);
+/* `steps` Adam steps (lr, betas 0.9 / 0.999) on minibatches of `batch`
+ * samples drawn with replacement from the n device samples; loss_hist
+ * (host, may be NULL) receives each step's sum|r*y - t|^2 / sum r^2. */
+int dc_gb300_mlp_train(dc_gb300_mlp *mlp, const float *samples, const float *targets,
+                       long long n, int steps, int batch, float lr, unsigned long long seed,
+                       float *loss_hist);
+/* The layer cells of a padded box (sx, sy, sz) with a layer `layer` cells
+ * wide, in the order the kernels use: cells[4*i..4*i+3] = x, y, z and
+ * axis | side << 2 | depth << 3 (axis of the normal, side 1 = high end,
+ * depth 0 = next to the interior).  Writes at most `cap` entries (cells may
+ * be NULL) and returns the count, or -1 on invalid geometry.  Host only. */
+long long dc_gb300_layer_cells(long sx, long sy, long sz, int layer, int *cells, long long cap);
+/* Applies the MLP after every stencil pass of dc_gb300_run to the layer
+ * cells of a layer `layer` cells wide (1..DC_GB300_MLP_DEPTHS; 0 turns it
+ * off).  The simulation reads the MLP's parameters at every step: keep the
+ * MLP alive while it is set. */
+int dc_gb300_set_learned_layer(dc_gb300_sim *sim, const dc_gb300_mlp *mlp, int layer);
+/* Teacher-forced training samples: the fields of `wide` (t and t-1) are
+ * cropped at offset[] to the box of `thin` (zero halo), `thin` steps once
+ * (its own sponge, no source, no learned layer) and `wide` steps once; each
+ * layer cell of `thin` appends a sample (features of the thin step, depth)
+ * to the device array samples[cap][33] and a target (wide field at t+1
+ * minus the thin step) to targets[cap][2].  *count = samples written. */
+int dc_gb300_lb_sample(dc_gb300_sim *wide, dc_gb300_sim *thin, const long offset[3], int layer,
+                       float *samples, float *targets, long long cap, long long *count);
+/* Rollout samples (training on the states the layer itself produces): the
+ * fields of `wide` are cropped into `thin` once, then `steps` times `thin`
+ * steps with its learned layer (recording each layer cell's features before
+ * its correction) and `wide` steps; targets are the wide field minus the
+ * thin stencil's output.  `thin` must have a learned layer and no source.
+ * Writes steps x (layer cells) samples; *count = that number. */
+int dc_gb300_lb_rollout(dc_gb300_sim *wide, dc_gb300_sim *thin, const long offset[3], int steps,
+                        float *samples, float *targets, long long cap, long long *count);
+
 /* Runs `steps` time steps of the exact kernel (reference arithmetic, no
  * source, no sponge) over caller-owned device buffers and allocates no
  * device memory.  No counterpart in the reference: it serves callers that
