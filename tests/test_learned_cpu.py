@@ -53,7 +53,7 @@ def _layer_cells_direct(s, layer):
 def test_layer_cell_table_matches_direct_enumeration(dc):
     """The library's layer-cell table: one entry per cell of the shell, with
     the normal axis, side and depth of a direct enumeration."""
-    s, layer = (26, 28, 27), 6
+    s, layer = (28, 30, 29), 6
     want = _layer_cells_direct(s, layer)
     got = dc.layer_cells(s, layer)
     # the corrected cells: the 4 outer cells of the layer on every side
