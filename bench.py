@@ -33,6 +33,15 @@ per shot; tile rows and z-split chosen by the library's autotuner.  One step
 advances every shot (one persistent launch); K defaults to 1000 steps.
 ``value`` is shot-point-updates per second summed over the shots.
 
+Learned form (--form learned): a 384^3 interior with the 8-cell learned
+absorbing layer (network weights from the package's data/learned_layer8.npy,
+trained by dc_gb300.learned.main) against the same interior with the
+48-cell sponge, K = 1500 steps, FP32, the same seeded medium generator.
+``value`` is interior point-updates per second of the learned form; the
+line also carries the sponge form's rate and the reflected energy of both
+in a 32-cell band next to the interior's boundary against a wide run whose
+reflections never return (sampled every 100 steps).
+
 Reference arm (--impl reference): the reference's CPU implementation of the
 path (the oracle port of src/openmp_propagate.c, all host threads) on the
 same workload; each step is one time step of a 608 x 608 x 16 slab.
@@ -71,6 +80,8 @@ BATCH_SHOTS = 64
 BATCH_DEPTH = 256
 BATCH_SEED = 2027
 BATCH_RECEIVERS = 64
+# learned form
+LEARNED_N, LEARNED_LAYER = 384, 8
 
 
 def parse():
@@ -86,11 +97,11 @@ def parse():
     ap.add_argument("--n", type=int, default=N_INTERIOR, help="interior cells per axis")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--form", choices=("plain", "batched"), default="plain")
+    ap.add_argument("--form", choices=("plain", "batched", "learned"), default="plain")
     ap.add_argument("--shots", type=int, default=BATCH_SHOTS)
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = 1000 if args.form == "batched" else 2000
+        args.steps = {"batched": 1000, "learned": 1500}.get(args.form, 2000)
     return args
 
 
@@ -581,6 +592,89 @@ def run_batched(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def run_learned(args, rank, world, local):
+    """The learned thin layer against the 48-cell sponge on one shot."""
+    import torch
+    import __graft_entry__ as ge
+    dc = ge.package()
+    dc.build()
+    from dc_gb300 import learned
+    torch.cuda.set_device(local)
+    n, layer = LEARNED_N, LEARNED_LAYER
+    st = learned.Setup(n=(n,) * 3, layer=layer, fcut=FCUT)
+    total = args.warmup + args.steps
+    src = (4 + layer + n // 2 + 8 * rank, 4 + layer + n // 2, 4 + layer + SRC_DEPTH)
+    mlp = dc.MLP(device=local, params=np.load(learned.WEIGHTS))
+
+    def timed(sim):
+        sim.run(args.warmup)
+        sim.synchronize()
+        stream = torch.cuda.ExternalStream(sim.stream)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = sim.launches
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        sim.run(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        sim.synchronize()
+        return ev0.elapsed_time(ev1), sim.launches - l0
+
+    def with_source(sim, sizes, s):
+        sx, sy, _ = sizes
+        sim.set_source(s[0] + s[1] * sx + s[2] * sx * sy, dc.source_table(DT, total + 2, FCUT))
+
+    thin = learned.thin_sim(st, local)
+    with_source(thin, st.thin_sizes, src)
+    dc.set_learned_layer(thin, mlp, layer)
+    with ClockSampler(local) as clk:
+        ms_l, launches = timed(thin)
+    thin.close()
+    a = ABSORB
+    sp = dc.Simulation(st.sponge_sizes, (DX,) * 3, DT, kernel=dc.KERNEL_FAST, device=local)
+    shift = st.wide_pad + layer - a
+    sp.generate_layered(learned._origin_spec(st, (shift,) * 3))
+    sp.set_fields()
+    sp.set_sponge(*[dc.sponge_profile(v, a, SPONGE_KAPPA) for v in st.sponge_sizes])
+    with_source(sp, st.sponge_sizes, tuple(c - layer + a for c in src))
+    ms_s, _ = timed(sp)
+    sp.close()
+    interior = n ** 3
+    value = interior * args.steps / (ms_l * 1e-3) / 1e9
+    sponge_value = interior * args.steps / (ms_s * 1e-3) / 1e9
+    refl = learned.reflected_energy(st, mlp, src, total, 100, 32, local)
+    mlp.close()
+    pts_l = (n + 2 * layer) ** 3
+    achieved = BYTES_PER_UPDATE * pts_l / (ms_l / args.steps * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_l / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded 12-layer TTI medium, numpy PCG64 seed 2026, generated on GPU)",
+        "config": {"workload": f"learned thin layer: {n}^3 interior, {layer}-cell learned layer "
+                               f"vs {ABSORB}-cell sponge, dt 0.8 ms, 20 Hz Ricker, FP32",
+                   "form": "learned", "value_counts": "interior point-updates",
+                   "learned": {"interior_gupd_s": value, "ms_per_step": ms_l / args.steps,
+                               "compute_points": pts_l},
+                   "sponge48": {"interior_gupd_s": sponge_value, "ms_per_step": ms_s / args.steps,
+                                "compute_points": (n + 2 * ABSORB) ** 3},
+                   "speedup_vs_sponge48": ms_s / ms_l,
+                   "reflected_energy_band32": refl,
+                   "global_batch": world, "seq_len": None, "parallelism": "single",
+                   "l2": "inputs ~4 GB >> 129 MB L2; no flush"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "bytes_per_update": BYTES_PER_UPDATE,
+                     "note": "stencil bytes over the whole learned step (stencil + network)",
+                     "traffic": None},
+        "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -589,6 +683,9 @@ def main():
         return
     if args.form == "batched":
         run_batched(args, rank, world, local)
+        return
+    if args.form == "learned":
+        run_learned(args, rank, world, local)
         return
     run_ours(args, rank, world, local)
 

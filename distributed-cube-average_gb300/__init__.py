@@ -495,6 +495,12 @@ class Simulation:
         check(lib().dc_gb300_get_fields(self.h, *[fptr(a) for a in out]))
         return dict(zip(("pp", "pc", "qp", "qc"), out))
 
+    def get_pc(self) -> np.ndarray:
+        """The current p field alone (dense)."""
+        out = np.empty(self.shape, np.float32)
+        check(lib().dc_gb300_get_fields(self.h, None, fptr(out), None, None))
+        return out
+
     def set_source(self, index: int, amplitudes) -> None:
         if index is None or index < 0:
             check(lib().dc_gb300_set_source(self.h, -1, None, 0))

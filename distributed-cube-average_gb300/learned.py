@@ -261,8 +261,7 @@ def _band_mask(n, band):
     return dist < band
 
 
-def _interior(fields, pad, n):
-    a = fields["pc"]
+def _interior(a, pad, n):
     return a[pad:pad + n[2], pad:pad + n[1], pad:pad + n[0]]
 
 
@@ -281,7 +280,7 @@ def reflected_energy(setup: Setup, mlp: MLP | None, src, steps: int, every: int,
         wide.run(k - done)
         done = k
         wide.synchronize()
-        truth[k] = _interior(wide.get_fields(), setup.wide_pad + 4 + setup.layer, setup.n).copy()
+        truth[k] = _interior(wide.get_pc(), setup.wide_pad + 4 + setup.layer, setup.n).copy()
     wide.close()
     ref = sum(float(np.sum(truth[k][mask].astype(np.float64) ** 2)) for k in keys)
 
@@ -291,7 +290,7 @@ def reflected_energy(setup: Setup, mlp: MLP | None, src, steps: int, every: int,
             sim.run(k - dn)
             dn = k
             sim.synchronize()
-            d = _interior(sim.get_fields(), pad, setup.n) - truth[k]
+            d = _interior(sim.get_pc(), pad, setup.n) - truth[k]
             err += float(np.sum(d[mask].astype(np.float64) ** 2))
         return err / ref if ref > 0 else float("nan")
 
@@ -323,3 +322,32 @@ def reflected_energy(setup: Setup, mlp: MLP | None, src, steps: int, every: int,
     out["sponge"] = run(sim, 4 + a)
     sim.close()
     return out
+
+
+WEIGHTS = __import__("pathlib").Path(__file__).resolve().parent / "data" / "learned_layer8.npy"
+
+
+def main(argv=None):
+    """Trains the layer's network (best of several seeds on validation
+    shots) and writes its parameters:
+
+        python -c "import __graft_entry__ as g; g.package(); \\
+                   from dc_gb300 import learned; learned.main(['--out', 'w.npy'])"
+    """
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(prog="learned")
+    ap.add_argument("--out", default=str(WEIGHTS))
+    ap.add_argument("--seeds", type=int, nargs="+", default=[11, 12, 13, 14])
+    ap.add_argument("--rounds", type=int, default=4)
+    ap.add_argument("--n", type=int, default=48)
+    ap.add_argument("--steps", type=int, default=320)
+    args = ap.parse_args(argv)
+    st = Setup(n=(args.n,) * 3, layer=8)
+    mlp, report = select(st, args.seeds, random_sources(st, 4, 7), random_sources(st, 2, 55),
+                         steps=args.steps, rounds=args.rounds)
+    if mlp is None:
+        raise SystemExit("no network beat the thin layer without it")
+    np.save(args.out, mlp.params())
+    mlp.close()
+    print(json.dumps({"out": args.out, "setup": str(st), "selection": report}))
