@@ -99,6 +99,14 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", choices=("plain", "batched", "learned"), default="plain")
     ap.add_argument("--shots", type=int, default=BATCH_SHOTS)
+    ap.add_argument("--model", type=int, nargs=3, default=list(BATCH_MODEL),
+                    help="batched form: model sizes (x y z); smaller for profiling captures")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batched form: keep the default tiles (profiling captures)")
+    ap.add_argument("--learned-n", type=int, default=LEARNED_N,
+                    help="learned form: interior cells per axis")
+    ap.add_argument("--no-judge", action="store_true",
+                    help="learned form: skip the reflected-energy judge")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"batched": 1000, "learned": 1500}.get(args.form, 2000)
@@ -473,24 +481,24 @@ def run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_over_ran
                                   "dc_device_data_get_results), pinned host buffers"}
 
 
-def batch_shots(n_shots: int, seed: int = BATCH_SEED):
+def batch_shots(n_shots: int, seed: int = BATCH_SEED, model=BATCH_MODEL):
     """Shot layout of the batched workload: sources on an 8 x 8 grid over the
     model surface with seeded jitter; each shot a crop of uneven aperture
     around its source.  Returns a list of dicts in medium-box coordinates."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    mx, my, mz = BATCH_MODEL
+    mx, my, mz = model
     side = 8
     shots = []
     for k in range(n_shots):
         i, j = (k % (side * side)) % side, (k % (side * side)) // side
         sx_m = int(mx * (i + 0.5) / side + rng.uniform(-mx / side / 4, mx / side / 4))
         sy_m = int(my * (j + 0.5) / side + rng.uniform(-my / side / 4, my / side / 4))
-        ax, ay = (int(v) for v in rng.integers(192, 321, size=2))
+        ax, ay = (min(int(v), m) for v, m in zip(rng.integers(192, 321, size=2), (mx, my)))
         peak = float(rng.uniform(15.0, 25.0))
         cx = min(max(sx_m - ax // 2, 0), mx - ax) // 4 * 4
         cy = min(max(sy_m - ay // 2, 0), my - ay)
         p = BATCH_PAD
-        sizes = (ax + 2 * p, ay + 2 * p, BATCH_DEPTH + 2 * p)
+        sizes = (ax + 2 * p, ay + 2 * p, min(BATCH_DEPTH, mz) + 2 * p)
         src = (sx_m - cx + p, sy_m - cy + p, p + SRC_DEPTH)
         rec_x = np.linspace(p, p + ax - 1, BATCH_RECEIVERS).astype(int)
         rec = [(int(x), src[1], p + 8) for x in rec_x]
@@ -515,15 +523,19 @@ def run_batched(args, rank, world, local):
     form = {"f32": dc.MEDIUM_PRECOMP, "f16": dc.MEDIUM_PRECOMP_F16,
             "bf16": dc.MEDIUM_PRECOMP_BF16}[args.medium if args.medium != "f32" else "f16"]
     storage = "f16" if args.medium == "f32" else args.medium
-    mbox = tuple(v + 2 * BATCH_PAD for v in BATCH_MODEL)
-    shots = batch_shots(args.shots, BATCH_SEED + rank)
+    model = tuple(args.model)
+    mbox = tuple(v + 2 * BATCH_PAD for v in model)
+    shots = batch_shots(args.shots, BATCH_SEED + rank, model)
     total = args.warmup + args.steps
     b = dc.Batch(mbox, (DX,) * 3, DT, medium=form, device=local, max_steps=total + 1)
     b.generate_layered(medium.layered_spec(MEDIUM_SEED, mbox))
     for k, sh in enumerate(shots):
         b.add_shot(sh["sizes"], sh["origin"], sh["src"], sh["fcut"], ABSORB, SPONGE_KAPPA)
         b.set_receivers(k, sh["rec"])
-    ty, zsplit, tune_ms = b.autotune(3)
+    if args.no_autotune:
+        (ty, zsplit), tune_ms = b.tiles(), None
+    else:
+        ty, zsplit, tune_ms = b.autotune(3)
     pts = b.points
     b.run(args.warmup)
     b.synchronize()
@@ -572,8 +584,8 @@ def run_batched(args, rank, world, local):
         "data": "synthetic (seeded 12-layer TTI medium, numpy PCG64 seed 2026, generated on "
                 "GPU; shot layout PCG64 seed 2027)",
         "config": {"workload": f"batched: {args.shots} shots in one persistent launch per step "
-                               f"over a shared {BATCH_MODEL[0]}x{BATCH_MODEL[1]}x"
-                               f"{BATCH_MODEL[2]} medium, crops U(192,320)^2 x {BATCH_DEPTH} "
+                               f"over a shared {model[0]}x{model[1]}x"
+                               f"{model[2]} medium, crops U(192,320)^2 x {BATCH_DEPTH} "
                                f"+ {ABSORB}-cell sponge, dt 0.8 ms, 15-25 Hz Ricker",
                    "form": "batched", "medium_storage": storage, "shots": args.shots,
                    "points_per_step": pts, "tiles": {"ty": ty, "zsplit": zsplit,
@@ -600,7 +612,7 @@ def run_learned(args, rank, world, local):
     dc.build()
     from dc_gb300 import learned
     torch.cuda.set_device(local)
-    n, layer = LEARNED_N, LEARNED_LAYER
+    n, layer = args.learned_n, LEARNED_LAYER
     st = learned.Setup(n=(n,) * 3, layer=layer, fcut=FCUT)
     total = args.warmup + args.steps
     src = (4 + layer + n // 2 + 8 * rank, 4 + layer + n // 2, 4 + layer + SRC_DEPTH)
@@ -642,7 +654,8 @@ def run_learned(args, rank, world, local):
     interior = n ** 3
     value = interior * args.steps / (ms_l * 1e-3) / 1e9
     sponge_value = interior * args.steps / (ms_s * 1e-3) / 1e9
-    refl = learned.reflected_energy(st, mlp, src, total, 100, 32, local)
+    refl = (None if args.no_judge else
+            learned.reflected_energy(st, mlp, src, total, 100, 32, local))
     mlp.close()
     pts_l = (n + 2 * layer) ** 3
     achieved = BYTES_PER_UPDATE * pts_l / (ms_l / args.steps * 1e-3) / 1e9
