@@ -185,6 +185,7 @@ SIGNATURES = [
     ("dc_gb300_batch_add_shot", C.c_int, [C.c_void_p, C.POINTER(Shot), C.POINTER(C.c_int)]),
     ("dc_gb300_batch_set_receivers", C.c_int,
      [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_long)]),
+    ("dc_gb300_batch_set_learned_layer", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     ("dc_gb300_batch_set_tiles", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("dc_gb300_batch_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("dc_gb300_batch_autotune", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int),
@@ -631,6 +632,10 @@ class Batch:
         arr = (C.c_long * max(1, a.size))(*a.reshape(-1).tolist())
         check(lib().dc_gb300_batch_set_receivers(self.h, int(shot), int(a.shape[0]), arr))
         self.nrec[shot] = int(a.shape[0])
+
+    def set_learned_layer(self, mlp: "MLP | None", layer: int) -> None:
+        check(lib().dc_gb300_batch_set_learned_layer(self.h, mlp.h if mlp is not None else None,
+                                                     int(layer)))
 
     def set_tiles(self, ty: int, zsplit: int) -> None:
         check(lib().dc_gb300_batch_set_tiles(self.h, int(ty), int(zsplit)))

@@ -69,6 +69,13 @@ struct Batch {
   int src_applied_step = -1;
   long launches = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // learned thin layer on every shot (after each step's stencil launches)
+  const float *lb_params = nullptr;
+  int lb_layer = 0;
+  int4 *d_lb_cells = nullptr;
+  float2 *d_lb_corr = nullptr;
+  LbShot *d_lb_shots = nullptr;
+  long long lb_cells = 0;
 };
 
 int fail(int code, const std::string &msg) {
@@ -116,6 +123,9 @@ void release(Batch *b) {
     cudaFree(s.pq[0]);
     cudaFree(s.pq[1]);
   }
+  cudaFree(b->d_lb_cells);
+  cudaFree(b->d_lb_corr);
+  cudaFree(b->d_lb_shots);
   cudaFree(b->coef);
   cudaFree(b->coef16);
   cudaFree(b->d_step);
@@ -320,6 +330,11 @@ cudaError_t queue_launches(Batch *b, int cur, int j) {
     const cudaError_t e = launch_batch(b->stream, bl, b->ty, b->coef_form, iso, b->blocks);
     if (e != cudaSuccess) return e;
   }
+  if (b->lb_cells > 0) {  // learned layer of every shot, after all stencil launches
+    b->launches += 2;
+    return launch_lb_batch_step(b->stream, b->lb_params, b->d_lb_cells, b->lb_cells,
+                                b->d_lb_shots, cur, b->d_lb_corr);
+  }
   return cudaSuccess;
 }
 
@@ -394,7 +409,8 @@ int run_steps(Batch *b, int steps) {
         return fail(DC_GB300_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
     }
     BATCH_TRY(cudaGraphLaunch(b->graph[cur], b->stream));
-    b->launches += static_cast<long>(kGraphSteps) * static_cast<long>(b->groups.size()) + 1;
+    b->launches += static_cast<long>(kGraphSteps) *
+                       (static_cast<long>(b->groups.size()) + (b->lb_cells > 0 ? 2 : 0)) + 1;
     left -= kGraphSteps;
     b->steps_done += kGraphSteps;
   }
@@ -567,6 +583,8 @@ extern "C" int dc_gb300_batch_set_precomp(dc_gb300_batch *h, const dc_precomp_va
 extern "C" int dc_gb300_batch_add_shot(dc_gb300_batch *h, const dc_gb300_shot *shot, int *index) {
   Batch *b = dcg::impl(h);
   if (!b || !shot) return fail(DC_GB300_ERR_ARG, "null argument");
+  if (b->lb_cells > 0)
+    return fail(DC_GB300_ERR_STATE, "add every shot before setting the learned layer");
   const dc_gb300_shot &c = *shot;
   if (c.sx < 9 || c.sy < 9 || c.sz < 9)
     return fail(DC_GB300_ERR_ARG, "every padded shot size must be at least 9");
@@ -605,6 +623,7 @@ extern "C" int dc_gb300_batch_add_shot(dc_gb300_batch *h, const dc_gb300_shot *s
   BATCH_TRY(cudaStreamSynchronize(b->stream));
   b->shots.push_back(std::move(s));
   if (index) *index = static_cast<int>(b->shots.size()) - 1;
+
   b->prepared = false;
   dcg::drop_graphs(b);
   return DC_GB300_OK;
@@ -646,6 +665,55 @@ extern "C" int dc_gb300_batch_set_receivers(dc_gb300_batch *h, int shot, int cou
   s.nrec = count;
   cudaSetDevice(b->device);
   dcg::free_tables(b);  // traces restart from zero
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_batch_set_learned_layer(dc_gb300_batch *h, const dc_gb300_mlp *mlp,
+                                                int layer) {
+  Batch *b = dcg::impl(h);
+  if (!b) return fail(DC_GB300_ERR_ARG, "null batch");
+  if (layer < 0 || layer > DC_GB300_MLP_DEPTHS)
+    return fail(DC_GB300_ERR_ARG, "layer width must lie in [0, DC_GB300_MLP_DEPTHS]");
+  if (layer > 0 && !mlp) return fail(DC_GB300_ERR_ARG, "null MLP");
+  BATCH_TRY(cudaSetDevice(b->device));
+  BATCH_TRY(cudaStreamSynchronize(b->stream));
+  dcg::drop_graphs(b);
+  cudaFree(b->d_lb_cells);
+  cudaFree(b->d_lb_corr);
+  cudaFree(b->d_lb_shots);
+  b->d_lb_cells = nullptr;
+  b->d_lb_corr = nullptr;
+  b->d_lb_shots = nullptr;
+  b->lb_cells = 0;
+  b->lb_layer = 0;
+  b->lb_params = nullptr;
+  if (layer == 0) return DC_GB300_OK;
+  if (b->shots.size() > (1u << 23)) return fail(DC_GB300_ERR_ARG, "too many shots");
+  std::vector<int4> cells;
+  std::vector<dcg::LbShot> tab;
+  for (size_t k = 0; k < b->shots.size(); ++k) {
+    const dcg::BShot &s = b->shots[k];
+    if (s.cfg.sx < 2 * layer + 16 || s.cfg.sy < 2 * layer + 16 || s.cfg.sz < 2 * layer + 16)
+      return fail(DC_GB300_ERR_ARG, "every shot's interior must keep at least 8 cells per axis");
+    const std::vector<int4> c = dcg::layer_cells(s.cfg.sx, s.cfg.sy, s.cfg.sz, layer);
+    for (int4 v : c) {
+      v.w |= static_cast<int>(k) << 8;
+      cells.push_back(v);
+    }
+    tab.push_back(dcg::LbShot{{s.pq[0], s.pq[1]}, s.pitch, s.plane});
+  }
+  const long long n = static_cast<long long>(cells.size());
+  BATCH_TRY(cudaMalloc(&b->d_lb_cells, sizeof(int4) * n));
+  BATCH_TRY(cudaMalloc(&b->d_lb_corr, sizeof(float2) * n));
+  BATCH_TRY(cudaMalloc(&b->d_lb_shots, sizeof(dcg::LbShot) * tab.size()));
+  BATCH_TRY(cudaMemcpyAsync(b->d_lb_cells, cells.data(), sizeof(int4) * n,
+                            cudaMemcpyHostToDevice, b->stream));
+  BATCH_TRY(cudaMemcpyAsync(b->d_lb_shots, tab.data(), sizeof(dcg::LbShot) * tab.size(),
+                            cudaMemcpyHostToDevice, b->stream));
+  BATCH_TRY(cudaStreamSynchronize(b->stream));
+  b->lb_cells = n;
+  b->lb_layer = layer;
+  b->lb_params = dc_gb300_mlp_device_params(mlp);
   return DC_GB300_OK;
 }
 

@@ -286,6 +286,13 @@ cudaError_t launch_lb_sample(cudaStream_t st, const int4 *cells, long long n, co
                              const float2 *cur, long long pitch, long long plane,
                              const float2 *wide, long long wpitch, long long wplane,
                              const int off[3], float *xs, float *ts);
+// Learned layer over a batch: cells carry their shot in meta bits 8..31.
+struct LbShot {
+  float2 *pq[2];              // the shot's pair buffers
+  long long pitch, plane;
+};
+cudaError_t launch_lb_batch_step(cudaStream_t st, const float *params, const int4 *cells,
+                                 long long n, const LbShot *shots, int cur_buf, float2 *corr);
 // Thin pair buffer <- box of a wide pair buffer at `off`, zero halo.
 cudaError_t launch_crop(cudaStream_t st, float2 *dst, long long sx, long long sy, long long sz,
                         long long pitch, const float2 *src, long long wpitch, long long wplane,

@@ -409,6 +409,44 @@ __global__ void __launch_bounds__(128) lb_infer_kernel(const float *__restrict__
   }
 }
 
+// Batch variant: the shot of cell i is meta >> 8; its new field is in
+// buffer 1 - cur_buf, its current field in cur_buf.
+__global__ void __launch_bounds__(128) lb_infer_batch_kernel(const float *__restrict__ wc,
+                                                             const int4 *__restrict__ cells,
+                                                             long long n,
+                                                             const LbShot *__restrict__ shots,
+                                                             int cur_buf, float2 *corr) {
+  __shared__ float sw[kParams];
+  load_params(sw, wc);
+  __syncthreads();
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    int4 c = cells[i];
+    const LbShot sh = shots[c.w >> 8];
+    c.w &= 0xff;
+    float x[kIn];
+    const int depth = gather(c, sh.pq[1 - cur_buf], sh.pq[cur_buf], sh.pitch, sh.plane, x);
+    float y[kOut];
+    const float r = forward(sw, x, depth, y);
+    corr[i] = make_float2(r * y[0], r * y[1]);
+  }
+}
+
+__global__ void lb_add_batch_kernel(const int4 *__restrict__ cells, long long n,
+                                    const LbShot *__restrict__ shots, int cur_buf,
+                                    const float2 *__restrict__ corr) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int4 c = cells[i];
+    const LbShot sh = shots[c.w >> 8];
+    float2 *nw = sh.pq[1 - cur_buf];
+    const long long g = static_cast<long long>(c.z) * sh.plane +
+                        static_cast<long long>(c.y) * sh.pitch + c.x;
+    const float2 d = corr[i], v = nw[g];
+    nw[g] = make_float2(v.x + d.x, v.y + d.y);
+  }
+}
+
 __global__ void lb_add_kernel(const int4 *__restrict__ cells, long long n, float2 *nw,
                               const float2 *__restrict__ corr, long long pitch, long long plane) {
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
@@ -531,6 +569,15 @@ cudaError_t launch_lb_step(cudaStream_t st, const float *wc, const int4 *cells, 
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   lb_add_kernel<<<grid_for(n, 256), 256, 0, st>>>(cells, n, nw, corr, pitch, plane);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lb_batch_step(cudaStream_t st, const float *wc, const int4 *cells,
+                                 long long n, const LbShot *shots, int cur_buf, float2 *corr) {
+  lb_infer_batch_kernel<<<grid_for(n, 128), 128, 0, st>>>(wc, cells, n, shots, cur_buf, corr);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  lb_add_batch_kernel<<<grid_for(n, 256), 256, 0, st>>>(cells, n, shots, cur_buf, corr);
   return cudaGetLastError();
 }
 

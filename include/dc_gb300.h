@@ -397,6 +397,12 @@ int dc_gb300_batch_add_shot(dc_gb300_batch *batch, const dc_gb300_shot *shot, in
 /* Receivers of one shot as (x, y, z) triples in box coordinates; traces
  * (p before the next step's source, [step][receiver]) restart from zero. */
 int dc_gb300_batch_set_receivers(dc_gb300_batch *batch, int shot, int count, const long *xyz);
+/* Applies a learned thin absorbing layer `layer` cells wide (see Part 4)
+ * to every shot after each step (0 turns it off).  Set it after adding
+ * every shot: dc_gb300_batch_add_shot fails while a layer is set. */
+struct dc_gb300_mlp;
+int dc_gb300_batch_set_learned_layer(dc_gb300_batch *batch, const struct dc_gb300_mlp *mlp,
+                                     int layer);
 /* Tile rows (8 or 16) and z-chunks per column (1..64). */
 int dc_gb300_batch_set_tiles(dc_gb300_batch *batch, int ty, int zsplit);
 int dc_gb300_batch_tiles(const dc_gb300_batch *batch, int *ty, int *zsplit);

@@ -192,3 +192,34 @@ def test_batch_rejects_bad_shots(dc, medium_coef):
             b.add_shot((40, 40, 40), (0, 0, 0), (2, 20, 20))     # source in the halo
         with pytest.raises(dc.DcError):
             b.run(1)                                             # no medium, no shots
+
+
+def test_batch_learned_layer_matches_single_simulation(dc, medium_coef):
+    """The learned thin layer applied to every shot of a batch gives each
+    shot exactly what a single-shot simulation with the same layer gives."""
+    from dc_gb300 import learned
+    layer = 8
+    params = np.load(learned.WEIGHTS)
+    shots = SHOTS[:2]
+    with dc.MLP(device=0, params=params) as mlp:
+        with dc.Batch(MEDIUM, D, DT, device=0, max_steps=STEPS + 2) as b:
+            b.set_precomp(medium_coef)
+            for sizes, origin, src, fcut in shots:
+                b.add_shot(sizes, origin, src, fcut, 0, 0.0)
+            b.set_learned_layer(mlp, layer)
+            with pytest.raises(dc.DcError):
+                b.add_shot(*shots[0][:4])  # shots first, then the layer
+            b.run(STEPS)
+            b.synchronize()
+            got = [b.get_fields(i) for i in range(len(shots))]
+        for (sizes, origin, src, fcut), g in zip(shots, got):
+            with dc.Simulation(sizes, D, DT, kernel=dc.KERNEL_FAST, device=0) as sim:
+                sim.set_precomp([crop(c, origin, sizes) for c in medium_coef])
+                sim.set_fields()
+                sim.set_source(dense_index(sizes, src), wavelet(dc, fcut, STEPS + 3))
+                dc.set_learned_layer(sim, mlp, layer)
+                sim.run(STEPS)
+                sim.synchronize()
+                want = sim.get_fields()
+            assert np.array_equal(g["pc"], want["pc"]) and np.array_equal(g["qc"], want["qc"])
+            assert np.abs(g["pc"]).max() > 0
