@@ -12,9 +12,12 @@
 //   scale     r = rms of the 32 features; the network sees x / r and its
 //             output is multiplied by r (the correction is homogeneous of
 //             degree 1 in the wavefield, like a linear absorbing condition)
-//   network   32 -> 32 -> 32 -> 2, GELU, BF16 weights and activations, FP32
-//             accumulation; the first hidden layer's bias depends on the
-//             cell's depth in the layer (0 = next to the interior)
+//   network   32 -> 32 -> 32 -> 2, GELU (tanh form), BF16 weights and
+//             activations, FP32 accumulation; the first hidden layer's bias
+//             depends on the cell's depth in the layer (0 = next to the
+//             interior).  Inference runs on the tensor cores (mma.sync
+//             m16n8k16 BF16, activations kept in registers between layers);
+//             training on CUDA cores.
 //
 // The normal of an edge or corner cell is the axis along which it lies
 // deepest in the layer (lowest axis on ties).
@@ -65,64 +68,34 @@ __device__ __forceinline__ float bf16r(float v) {
   return __bfloat162float(__float2bfloat16_rn(v));
 }
 
+// GELU in its tanh form (Hendrycks & Gimpel 2016):
+//   gelu(a) = a/2 (1 + tanh(c0 (a + c1 a^3))), c0 = sqrt(2/pi), c1 = 0.044715,
+// with the hardware tanh (tanh.approx.f32, one MUFU operation), the same in
+// training and inference.
+constexpr float kGeluC0 = 0.7978845608028654f, kGeluC1 = 0.044715f;
+
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ float gelu(float a) {
-  return 0.5f * a * (1.0f + erff(a * 0.70710678118654752f));
+  const float u = kGeluC0 * fmaf(kGeluC1 * a * a, a, a);
+  const float h = 0.5f * a;
+  return fmaf(h, tanh_hw(u), h);
 }
 
 __device__ __forceinline__ float gelu_grad(float a) {
-  const float cdf = 0.5f * (1.0f + erff(a * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * expf(-0.5f * a * a);
-  return cdf + a * pdf;
+  const float a2 = a * a;
+  const float th = tanh_hw(kGeluC0 * fmaf(kGeluC1 * a2, a, a));
+  const float du = kGeluC0 * fmaf(3.0f * kGeluC1, a2, 1.0f);
+  return 0.5f * (1.0f + th) + 0.5f * a * (1.0f - th * th) * du;
 }
 
 // Copies the compute parameters into shared memory.
 __device__ __forceinline__ void load_params(float *sw, const float *wc) {
   for (int i = threadIdx.x; i < kParams; i += blockDim.x) sw[i] = wc[i];
-}
-
-// Forward pass of one sample from raw features x[32] (r = rms, 0 if
-// silent); writes y[2] (network output before the r scaling).
-__device__ __forceinline__ float forward(const float *sw, const float *x, int depth, float y[kOut]) {
-  float ss = 0.0f;
-#pragma unroll
-  for (int k = 0; k < kIn; ++k) ss = fmaf(x[k], x[k], ss);
-  const float r = sqrtf(ss * (1.0f / kIn));
-  if (!(r > 0.0f)) {
-    y[0] = y[1] = 0.0f;
-    return 0.0f;
-  }
-  const float inv = 1.0f / r;
-  float xh[kIn];
-#pragma unroll
-  for (int k = 0; k < kIn; ++k) xh[k] = bf16r(x[k] * inv);
-  float h1[kHid];
-  const float *b1 = sw + OFF_B1 + depth * kHid;
-#pragma unroll 4
-  for (int o = 0; o < kHid; ++o) {
-    float a = b1[o];
-    const float *w = sw + OFF_W1 + o * kIn;
-#pragma unroll
-    for (int k = 0; k < kIn; ++k) a = fmaf(w[k], xh[k], a);
-    h1[o] = bf16r(gelu(a));
-  }
-  float h2[kHid];
-#pragma unroll 4
-  for (int o = 0; o < kHid; ++o) {
-    float a = sw[OFF_B2 + o];
-    const float *w = sw + OFF_W2 + o * kHid;
-#pragma unroll
-    for (int k = 0; k < kHid; ++k) a = fmaf(w[k], h1[k], a);
-    h2[o] = bf16r(gelu(a));
-  }
-#pragma unroll
-  for (int j = 0; j < kOut; ++j) {
-    float a = sw[OFF_B3 + j];
-    const float *w = sw + OFF_W3 + j * kHid;
-#pragma unroll
-    for (int k = 0; k < kHid; ++k) a = fmaf(w[k], h2[k], a);
-    y[j] = a;
-  }
-  return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -337,27 +310,6 @@ __global__ void mlp_round_kernel(const float *master, float *wc) {
   if (p < kParams) wc[p] = is_weight(p) ? bf16r(master[p]) : master[p];
 }
 
-// Network output (r * y: the correction) for n samples.
-__global__ void __launch_bounds__(128) mlp_forward_kernel(const float *__restrict__ wc,
-                                                          const float *__restrict__ xs,
-                                                          long long n, float *out) {
-  __shared__ float sw[kParams];
-  load_params(sw, wc);
-  __syncthreads();
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    float x[kIn];
-    const float *row = xs + i * kStride;
-#pragma unroll
-    for (int k = 0; k < kIn; ++k) x[k] = row[k];
-    const int depth = min(max(static_cast<int>(row[kIn]), 0), kDepths - 1);
-    float y[kOut];
-    const float r = forward(sw, x, depth, y);
-    out[i * kOut] = r * y[0];
-    out[i * kOut + 1] = r * y[1];
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Layer cells: int4 {x, y, z, meta}, meta = axis | side << 2 | depth << 3
 // (side 1 = the high end of the axis).
@@ -382,53 +334,220 @@ __device__ __forceinline__ int gather(const int4 c, const float2 *nw, const floa
   return depth;
 }
 
-// `rec` (may be null): the features and depth of every cell are also
-// written there as sample rows (rollout training).
-__global__ void __launch_bounds__(128) lb_infer_kernel(const float *__restrict__ wc,
-                                                       const int4 *__restrict__ cells,
-                                                       long long n, const float2 *nw,
-                                                       const float2 *cur, long long pitch,
-                                                       long long plane, float2 *corr,
-                                                       float *rec) {
-  __shared__ float sw[kParams];
-  load_params(sw, wc);
-  __syncthreads();
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    float x[kIn];
-    const int depth = gather(cells[i], nw, cur, pitch, plane, x);
-    if (rec) {
-      float *row = rec + i * kStride;
-#pragma unroll
-      for (int k = 0; k < kIn; ++k) row[k] = x[k];
-      row[kIn] = static_cast<float>(depth);
-    }
-    float y[kOut];
-    const float r = forward(sw, x, depth, y);
-    corr[i] = make_float2(r * y[0], r * y[1]);
-  }
+// ---------------------------------------------------------------------------
+// Inference on the tensor cores.  One warp evaluates 16 cells per pass with
+// mma.sync.m16n8k16 (BF16 operands, FP32 accumulation).  Lane (g = lane/4,
+// t = lane%4) holds rows g and g+8 -- two cells -- and, per cell, the
+// features of window positions 2t and 2t+1: exactly its A-fragment elements
+// of the first layer (feature order p(t+1)[0..7], q(t+1)[0..7], p(t)[0..7],
+// q(t)[0..7]).  Each layer's accumulator fragments are the next layer's A
+// fragments, so the activations never leave registers; the weights are
+// loaded once per warp as B fragments.
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t *>(&v);
 }
 
-// Batch variant: the shot of cell i is meta >> 8; its new field is in
-// buffer 1 - cur_buf, its current field in cur_buf.
-__global__ void __launch_bounds__(128) lb_infer_batch_kernel(const float *__restrict__ wc,
-                                                             const int4 *__restrict__ cells,
-                                                             long long n,
-                                                             const LbShot *__restrict__ shots,
-                                                             int cur_buf, float2 *corr) {
-  __shared__ float sw[kParams];
-  load_params(sw, wc);
-  __syncthreads();
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    int4 c = cells[i];
-    const LbShot sh = shots[c.w >> 8];
+__device__ __forceinline__ void mma_bf16(float d[4], const uint32_t a[4], uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Feature sources: load(r, t, f) fills f = {p1[2t], p1[2t+1], q1[2t],
+// q1[2t+1], p0[2t], p0[2t+1], q0[2t], q0[2t+1]} of cell / sample r (p1, q1
+// at t+1, p0, q0 at t) and returns its depth.
+struct RowSrc {  // sample rows [n][33]
+  const float *rows;
+  __device__ __forceinline__ int load(long long r, int t, float f[8]) const {
+    const float *row = rows + r * kStride;
+    f[0] = row[2 * t];
+    f[1] = row[2 * t + 1];
+    f[2] = row[kWin + 2 * t];
+    f[3] = row[kWin + 2 * t + 1];
+    f[4] = row[2 * kWin + 2 * t];
+    f[5] = row[2 * kWin + 2 * t + 1];
+    f[6] = row[3 * kWin + 2 * t];
+    f[7] = row[3 * kWin + 2 * t + 1];
+    return min(max(static_cast<int>(row[kIn]), 0), kDepths - 1);
+  }
+};
+
+__device__ __forceinline__ int load_cell(int4 c, const float2 *nw, const float2 *cur,
+                                         long long pitch, long long plane, int t, float f[8],
+                                         float *rec) {
+  const int axis = c.w & 3, side = (c.w >> 2) & 1, depth = (c.w >> 3) & 31;
+  const long long stride = axis == 0 ? 1 : axis == 1 ? pitch : plane;
+  const long long step = side ? -stride : stride;  // inward
+  const long long g = static_cast<long long>(c.z) * plane + static_cast<long long>(c.y) * pitch +
+                      c.x + step * (2 * t);
+  const float2 a0 = nw[g], a1 = nw[g + step], b0 = cur[g], b1 = cur[g + step];
+  f[0] = a0.x;
+  f[1] = a1.x;
+  f[2] = a0.y;
+  f[3] = a1.y;
+  f[4] = b0.x;
+  f[5] = b1.x;
+  f[6] = b0.y;
+  f[7] = b1.y;
+  if (rec) {  // rollout training: the sample row of this cell
+    rec[2 * t] = f[0];
+    rec[2 * t + 1] = f[1];
+    rec[kWin + 2 * t] = f[2];
+    rec[kWin + 2 * t + 1] = f[3];
+    rec[2 * kWin + 2 * t] = f[4];
+    rec[2 * kWin + 2 * t + 1] = f[5];
+    rec[3 * kWin + 2 * t] = f[6];
+    rec[3 * kWin + 2 * t + 1] = f[7];
+    if (t == 0) rec[kIn] = static_cast<float>(depth);
+  }
+  return depth;
+}
+
+struct CellSrc {  // the layer cells of one simulation
+  const int4 *cells;
+  const float2 *nw, *cur;
+  long long pitch, plane;
+  float *rec;
+  __device__ __forceinline__ int load(long long r, int t, float f[8]) const {
+    return load_cell(cells[r], nw, cur, pitch, plane, t, f, rec ? rec + r * kStride : nullptr);
+  }
+};
+
+struct BatchCellSrc {  // the layer cells of every shot of a batch
+  const int4 *cells;
+  const LbShot *shots;
+  int cur_buf;
+  __device__ __forceinline__ int load(long long r, int t, float f[8]) const {
+    int4 c = cells[r];
+    const LbShot &sh = shots[c.w >> 8];
     c.w &= 0xff;
-    float x[kIn];
-    const int depth = gather(c, sh.pq[1 - cur_buf], sh.pq[cur_buf], sh.pitch, sh.plane, x);
-    float y[kOut];
-    const float r = forward(sw, x, depth, y);
-    corr[i] = make_float2(r * y[0], r * y[1]);
+    return load_cell(c, sh.pq[1 - cur_buf], sh.pq[cur_buf], sh.pitch, sh.plane, t, f, nullptr);
+  }
+};
+
+template <class Src>
+__global__ void __launch_bounds__(128) lb_tc_kernel(const float *__restrict__ wc, Src src,
+                                                    long long n, float2 *out) {
+  __shared__ float sb1[kDepths * kHid], sb2[kHid], sb3[kOut];
+  for (int i = threadIdx.x; i < kDepths * kHid; i += blockDim.x) sb1[i] = wc[OFF_B1 + i];
+  if (threadIdx.x < kHid) sb2[threadIdx.x] = wc[OFF_B2 + threadIdx.x];
+  if (threadIdx.x < kOut) sb3[threadIdx.x] = wc[OFF_B3 + threadIdx.x];
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  // B fragments: B[k][n] = W[n][k] of each 16 x 8 (k x n) block
+  uint32_t w1[2][4][2], w2[2][4][2], w3[2][2];
+#pragma unroll
+  for (int kk = 0; kk < 2; ++kk) {
+    const int k0 = kk * 16 + 2 * t;
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const float *r1 = wc + OFF_W1 + (nt * 8 + g) * kIn;
+      const float *r2 = wc + OFF_W2 + (nt * 8 + g) * kHid;
+      w1[kk][nt][0] = pack_bf16(r1[k0], r1[k0 + 1]);
+      w1[kk][nt][1] = pack_bf16(r1[k0 + 8], r1[k0 + 9]);
+      w2[kk][nt][0] = pack_bf16(r2[k0], r2[k0 + 1]);
+      w2[kk][nt][1] = pack_bf16(r2[k0 + 8], r2[k0 + 9]);
+    }
+    const float *r3 = wc + OFF_W3 + min(g, kOut - 1) * kHid;
+    w3[kk][0] = g < kOut ? pack_bf16(r3[k0], r3[k0 + 1]) : 0u;
+    w3[kk][1] = g < kOut ? pack_bf16(r3[k0 + 8], r3[k0 + 9]) : 0u;
+  }
+  __syncthreads();
+  const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+  for (long long base = warp * 16; base < n; base += nwarps * 16) {
+    const long long r0 = base + g, r1 = base + g + 8;
+    float f0[8], f1[8];
+    int d0 = 0, d1 = 0;
+    if (r0 < n) {
+      d0 = src.load(r0, t, f0);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) f0[k] = 0.f;
+    }
+    if (r1 < n) {
+      d1 = src.load(r1, t, f1);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) f1[k] = 0.f;
+    }
+    // rms of each cell's 32 features (spread over the 4 lanes of a quad)
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      s0 = fmaf(f0[k], f0[k], s0);
+      s1 = fmaf(f1[k], f1[k], s1);
+    }
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+    if (__all_sync(0xffffffffu, s0 == 0.f && s1 == 0.f)) {  // 16 silent cells: no correction
+      if (t == 0) {
+        if (r0 < n) out[r0] = make_float2(0.f, 0.f);
+        if (r1 < n) out[r1] = make_float2(0.f, 0.f);
+      }
+      continue;
+    }
+    const float rr0 = sqrtf(s0 * (1.0f / kIn)), rr1 = sqrtf(s1 * (1.0f / kIn));
+    const float i0 = rr0 > 0.f ? 1.0f / rr0 : 0.f, i1 = rr1 > 0.f ? 1.0f / rr1 : 0.f;
+    uint32_t a[2][4];
+#pragma unroll
+    for (int kk = 0; kk < 2; ++kk) {
+      a[kk][0] = pack_bf16(f0[4 * kk] * i0, f0[4 * kk + 1] * i0);
+      a[kk][1] = pack_bf16(f1[4 * kk] * i1, f1[4 * kk + 1] * i1);
+      a[kk][2] = pack_bf16(f0[4 * kk + 2] * i0, f0[4 * kk + 3] * i0);
+      a[kk][3] = pack_bf16(f1[4 * kk + 2] * i1, f1[4 * kk + 3] * i1);
+    }
+    float acc[4][4];
+    // layer 1 (bias per depth)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const int c = nt * 8 + 2 * t;
+      acc[nt][0] = sb1[d0 * kHid + c];
+      acc[nt][1] = sb1[d0 * kHid + c + 1];
+      acc[nt][2] = sb1[d1 * kHid + c];
+      acc[nt][3] = sb1[d1 * kHid + c + 1];
+      mma_bf16(acc[nt], a[0], w1[0][nt][0], w1[0][nt][1]);
+      mma_bf16(acc[nt], a[1], w1[1][nt][0], w1[1][nt][1]);
+    }
+#pragma unroll
+    for (int kk = 0; kk < 2; ++kk) {
+      a[kk][0] = pack_bf16(gelu(acc[2 * kk][0]), gelu(acc[2 * kk][1]));
+      a[kk][1] = pack_bf16(gelu(acc[2 * kk][2]), gelu(acc[2 * kk][3]));
+      a[kk][2] = pack_bf16(gelu(acc[2 * kk + 1][0]), gelu(acc[2 * kk + 1][1]));
+      a[kk][3] = pack_bf16(gelu(acc[2 * kk + 1][2]), gelu(acc[2 * kk + 1][3]));
+    }
+    // layer 2
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const int c = nt * 8 + 2 * t;
+      acc[nt][0] = acc[nt][2] = sb2[c];
+      acc[nt][1] = acc[nt][3] = sb2[c + 1];
+      mma_bf16(acc[nt], a[0], w2[0][nt][0], w2[0][nt][1]);
+      mma_bf16(acc[nt], a[1], w2[1][nt][0], w2[1][nt][1]);
+    }
+#pragma unroll
+    for (int kk = 0; kk < 2; ++kk) {
+      a[kk][0] = pack_bf16(gelu(acc[2 * kk][0]), gelu(acc[2 * kk][1]));
+      a[kk][1] = pack_bf16(gelu(acc[2 * kk][2]), gelu(acc[2 * kk][3]));
+      a[kk][2] = pack_bf16(gelu(acc[2 * kk + 1][0]), gelu(acc[2 * kk + 1][1]));
+      a[kk][3] = pack_bf16(gelu(acc[2 * kk + 1][2]), gelu(acc[2 * kk + 1][3]));
+    }
+    // layer 3: outputs in columns 0 and 1, held by the lanes with t == 0
+    float y[4];
+    y[0] = y[2] = t == 0 ? sb3[0] : 0.f;
+    y[1] = y[3] = t == 0 ? sb3[1] : 0.f;
+    mma_bf16(y, a[0], w3[0][0], w3[0][1]);
+    mma_bf16(y, a[1], w3[1][0], w3[1][1]);
+    if (t == 0) {
+      if (r0 < n) out[r0] = make_float2(rr0 * y[0], rr0 * y[1]);
+      if (r1 < n) out[r1] = make_float2(rr1 * y[2], rr1 * y[3]);
+    }
   }
 }
 
@@ -564,8 +683,8 @@ std::vector<int4> layer_cells(long long sx, long long sy, long long sz, int laye
 cudaError_t launch_lb_step(cudaStream_t st, const float *wc, const int4 *cells, long long n,
                            float2 *nw, const float2 *cur, long long pitch, long long plane,
                            float2 *corr, float *rec) {
-  lb_infer_kernel<<<grid_for(n, 128), 128, 0, st>>>(wc, cells, n, nw, cur, pitch, plane, corr,
-                                                    rec);
+  lb_tc_kernel<CellSrc><<<grid_for(n, 64), 128, 0, st>>>(
+      wc, CellSrc{cells, nw, cur, pitch, plane, rec}, n, corr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   lb_add_kernel<<<grid_for(n, 256), 256, 0, st>>>(cells, n, nw, corr, pitch, plane);
@@ -574,7 +693,8 @@ cudaError_t launch_lb_step(cudaStream_t st, const float *wc, const int4 *cells, 
 
 cudaError_t launch_lb_batch_step(cudaStream_t st, const float *wc, const int4 *cells,
                                  long long n, const LbShot *shots, int cur_buf, float2 *corr) {
-  lb_infer_batch_kernel<<<grid_for(n, 128), 128, 0, st>>>(wc, cells, n, shots, cur_buf, corr);
+  lb_tc_kernel<BatchCellSrc><<<grid_for(n, 64), 128, 0, st>>>(
+      wc, BatchCellSrc{cells, shots, cur_buf}, n, corr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   lb_add_batch_kernel<<<grid_for(n, 256), 256, 0, st>>>(cells, n, shots, cur_buf, corr);
@@ -735,7 +855,8 @@ extern "C" int dc_gb300_mlp_forward(dc_gb300_mlp *m, const float *samples, long 
   if (!m || (n > 0 && (!samples || !out))) return fail(DC_GB300_ERR_ARG, "null argument");
   if (n <= 0) return DC_GB300_OK;
   LB_TRY(cudaSetDevice(m->device));
-  dcg::mlp_forward_kernel<<<dcg::grid_for(n, 128), 128, 0, m->stream>>>(m->wc, samples, n, out);
+  dcg::lb_tc_kernel<dcg::RowSrc><<<dcg::grid_for(n, 64), 128, 0, m->stream>>>(
+      m->wc, dcg::RowSrc{samples}, n, reinterpret_cast<float2 *>(out));
   LB_TRY(cudaGetLastError());
   LB_TRY(cudaStreamSynchronize(m->stream));
   return DC_GB300_OK;

@@ -53,7 +53,8 @@ def test_mlp_gradient_matches_oracle(dc, torch):
         g, (le, lw) = m.gradient(xs.data_ptr(), ts.data_ptr(), len(s))
     gw, le_w, lw_w = mo.gradient(p, s, t)
     assert rel_l2(g, gw) <= 1e-3
-    assert abs(le - le_w) <= 1e-4 * le_w and abs(lw - lw_w) <= 1e-5 * lw_w
+    # the GPU's tanh is the hardware approximation (relative error ~2^-11)
+    assert abs(le - le_w) <= 1e-3 * le_w and abs(lw - lw_w) <= 1e-5 * lw_w
     for lo, hi in ((mo.OFF_W1, mo.OFF_B1), (mo.OFF_B1, mo.OFF_W2), (mo.OFF_W2, mo.OFF_B2),
                    (mo.OFF_W3, mo.NPARAMS)):
         assert rel_l2(g[lo:hi], gw[lo:hi]) <= 2e-3, (lo, hi)
