@@ -42,6 +42,10 @@ line also carries the sponge form's rate and the reflected energy of both
 in a 32-cell band next to the interior's boundary against a wide run whose
 reflections never return (sampled every 100 steps).
 
+Mixed-precision form (--form mixed): 1024 x 1024 x 768 interior + 48-cell
+sponge (1.084 G updated points per step), FP16 coefficient storage (BF16
+with --medium bf16), FP32 arithmetic and wavefields, K = 1500 steps.
+
 Best form (--form best): the batched workload's 64 crops with the 8-cell
 learned layer instead of the 48-cell sponge and FP16 medium storage, against
 the plain form (FP32, 48-cell sponge, one shot at a time through
@@ -104,7 +108,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_INTERIOR, help="interior cells per axis")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--form", choices=("plain", "batched", "learned", "best"), default="plain")
+    ap.add_argument("--form", choices=("plain", "mixed", "batched", "learned", "best"),
+                    default="plain")
     ap.add_argument("--shots", type=int, default=BATCH_SHOTS)
     ap.add_argument("--model", type=int, nargs=3, default=list(BATCH_MODEL),
                     help="batched form: model sizes (x y z); smaller for profiling captures")
@@ -116,7 +121,17 @@ def parse():
                     help="learned form: skip the reflected-energy judge")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = {"batched": 1000, "learned": 1500, "best": 1000}.get(args.form, 2000)
+        args.steps = {"batched": 1000, "learned": 1500, "best": 1000,
+                      "mixed": 1500}.get(args.form, 2000)
+    if args.form == "mixed":
+        # the mixed-precision workload: 1024 x 1024 x 768 interior + 48-cell
+        # sponge, FP16 medium unless another storage is asked for
+        args.nxyz = (1024, 1024, 768)
+        if args.medium == "f32":
+            args.medium = "f16"
+        args.no_e2e = True
+    else:
+        args.nxyz = (args.n,) * 3
     return args
 
 
@@ -207,9 +222,9 @@ def profiled_traffic(name: str):
     return None
 
 
-def geometry(n: int):
+def geometry(n):
     from dc_gb300.medium import Geometry
-    return Geometry((n, n, n), ABSORB)
+    return Geometry(tuple(n) if isinstance(n, (tuple, list)) else (n, n, n), ABSORB)
 
 
 def shot_source(geom, rank: int) -> int:
@@ -332,7 +347,7 @@ def run_ours(args, rank, world, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    geom = geometry(args.n)
+    geom = geometry(args.nxyz)
     sizes = geom.sizes
     pts = geom.compute_points
     kernel = dc.KERNEL_FAST if args.kernel == "fast" else dc.KERNEL_EXACT
@@ -375,7 +390,6 @@ def run_ours(args, rank, world, local):
     traffic_pp = (profiled_traffic("tti_fast_config2.md")
                   if kernel == dc.KERNEL_FAST and args.n == N_INTERIOR and args.medium == "f32"
                   else None)
-    out_fields = sim.get_fields() if not args.no_cpu_baseline else None
     sim.close()
 
     # ---- end to end through the reference ABI with host buffers ----------
@@ -395,7 +409,6 @@ def run_ours(args, rank, world, local):
         cpu = {"value": rate / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": f"{reps} oracle steps of a {ssizes[0] - 8}x{ssizes[1] - 8}x"
                          f"{ssizes[2] - 8} slab of the same workload ({el:.1f} s)"}
-        del out_fields
 
     if rank != 0:
         return
@@ -405,8 +418,14 @@ def run_ours(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded 12-layer TTI medium, numpy PCG64 seed 2026, generated on GPU)",
-        "config": {"workload": f"plain FP32 TTI, {args.n}^3 interior + {ABSORB}-cell sponge, "
-                               f"{geom.sizes[0]}^3 padded, dt 0.8 ms, 20 Hz Ricker",
+        "config": {"workload": (f"plain FP32 TTI, {args.n}^3 interior + {ABSORB}-cell sponge, "
+                                f"{geom.sizes[0]}^3 padded, dt 0.8 ms, 20 Hz Ricker")
+                   if args.form == "plain" else
+                   (f"mixed precision: {'x'.join(map(str, args.nxyz))} interior + "
+                    f"{ABSORB}-cell sponge, {args.medium.upper()} medium storage, FP32 math "
+                    f"and wavefields, dt 0.8 ms, 20 Hz Ricker; rel. L2 vs FP64 oracle "
+                    f"stated by tests/test_gpu_mixed.py"),
+                   "form": args.form,
                    "kernel": args.kernel, "medium_storage": args.medium,
                    "points_per_step": pts, "global_batch": world,
                    "seq_len": None, "parallelism": f"shots{world}" if world > 1 else "single",

@@ -212,6 +212,45 @@ def test_config1_500_steps_within_fp32_noise(dc, port):
     assert rel_l2(fast["pc"], f64.pc) <= 1.5 * ref_err + 1e-7
 
 
+def test_config1_homogeneous_workload(dc, port):
+    """The config-1 workload itself: 64^3 interior + 16-cell sponge,
+    homogeneous vp 3000, epsilon 0.24, delta 0.10, theta pi/4, phi pi/6,
+    vs 0, 15 Hz Ricker (FCUT 45) at the centre, dt 1 ms, 500 steps, final p
+    and a 64-receiver line at interior depth 8.  Exact: bit-identical to
+    the oracle's reference arithmetic (fields and traces); fast: 1e-4 of it
+    and no further from FP64 than 1.5x the reference's own FP32 distance."""
+    from dc_gb300 import medium
+    geom = Geometry((64, 64, 64), 16)
+    coef = port.precomp(medium.homogeneous(geom.sizes))
+    steps, dt, d = 500, 1e-3, (12.5, 12.5, 12.5)
+    src = port.source_table(dt, steps + 1, 45.0)
+    sponge = [port.sponge_profile(s, geom.absorb, 0.35) for s in geom.sizes]
+    rec = medium.receiver_line(medium.Geometry(geom.n, geom.absorb), 64, 8)
+    s = geom.source_index  # the centre s // 2
+    common = dict(coef=coef, src_index=s, src=src, sponge=sponge, rec=rec)
+    ref = port.run(KIND_F32, geom.sizes, d, dt, steps, *zeros(geom.shape), **common)
+    f64 = port.run(KIND_F64, geom.sizes, d, dt, steps, *zeros(geom.shape, np.float64), **common)
+    out = {}
+    for kernel in (dc.KERNEL_EXACT, dc.KERNEL_FAST):
+        with dc.Simulation(geom.sizes, d, dt, kernel=kernel, device=0) as sim:
+            sim.set_precomp(coef)
+            sim.set_fields()
+            sim.set_source(s, src)
+            sim.set_sponge(*sponge)
+            sim.set_receivers(rec, steps)
+            sim.run(steps)
+            sim.synchronize()
+            out[kernel] = (sim.get_fields(), sim.traces(steps))
+    ex, ex_tr = out[dc.KERNEL_EXACT]
+    assert np.array_equal(ex["pc"], ref.pc) and np.array_equal(ex["qc"], ref.qc)
+    assert np.array_equal(ex_tr, ref.traces.astype(np.float32))
+    fa, fa_tr = out[dc.KERNEL_FAST]
+    assert rel_l2(fa["pc"], ref.pc) <= 1e-4 and rel_l2(fa_tr, ref.traces) <= 1e-4
+    ref_err = rel_l2(ref.pc, f64.pc)
+    assert rel_l2(fa["pc"], f64.pc) <= 1.5 * ref_err + 1e-7
+    assert np.abs(fa_tr).max() > 0
+
+
 def test_ragged_and_tiny_cubes(dc, port):
     """Sizes that are not multiples of 4 (pitched rows), of the 32 x 16
     tile, and cubes below the 16-cell threshold of the reference's region
