@@ -44,17 +44,6 @@ long long round_up4(long long v) { return (v + 3) / 4 * 4; }
 
 Sim *impl(dc_gb300_sim *h) { return h ? h->impl : nullptr; }
 
-// Copies a dense host array (sx*sy*sz) into a pitched device array.
-cudaError_t upload_dense(Sim *s, float *dst, const float *src) {
-  return cudaMemcpy2DAsync(dst, s->pitch * 4, src, s->sx * 4, s->sx * 4,
-                           s->sy * s->sz, cudaMemcpyHostToDevice, s->stream);
-}
-
-cudaError_t download_dense(Sim *s, float *dst, const float *src) {
-  return cudaMemcpy2DAsync(dst, s->sx * 4, src, s->pitch * 4, s->sx * 4,
-                           s->sy * s->sz, cudaMemcpyDeviceToHost, s->stream);
-}
-
 // Pair buffer that holds the field whose p component is `p` and q component
 // `q` (q == p + 1), or -1.
 int pair_of(const Sim *s, const float *p, const float *q) {

@@ -6,8 +6,10 @@
 // Work decomposition: a CTA owns a 32 x TY column tile in (x, y) and sweeps
 // a chunk of output planes along z.  For the leading plane k it receives,
 // by TMA into a 3-deep shared-memory ring:
-//   * the (p, q) pairs of plane k with a 4-cell halo in x and y,
-//   * the coefficients and the (pp, qp) tile of the output plane z = k - 4.
+//   * the (p, q) pairs of plane k with a 4-cell halo in x and y and the
+//     in-plane coefficient group (cxx, cyy, cxy, czz) of plane k,
+//   * the other coefficients and the (pp, qp) tile of the output plane
+//     z = k - 4.
 // Each thread owns one (x, y) column and keeps, in registers, 9-deep queues
 // of (p, q) pairs: the centre value, the x-derivative and the y-derivative.
 // The cross derivatives are evaluated in their separable form: with the
@@ -17,8 +19,14 @@
 //   d2/dxdy = D_x of a shared-memory plane of the y-derivative,
 //   d2/dxdz = D_z of the x-derivative queue,
 //   d2/dydz = D_z of the y-derivative queue.
-// The in-plane second derivatives and d2/dxdy of plane k wait four planes in
-// a per-thread shared-memory ring until plane k is the output plane.
+// The in-plane part of H1 (cxx d2/dx2 + cyy d2/dy2 + cxy d2/dxdy), the
+// in-plane Laplacian and czz of plane k wait four planes in a per-thread
+// shared-memory ring (9 slots, indexed by the compile-time plane number)
+// until plane k is the output plane.
+//
+// The sweep of one column tile is `sweep_column`; `fast_kernel` runs one
+// tile per CTA over one box, `batch_kernel` runs persistent CTAs over the
+// tiles of many boxes (shots) cropped out of one shared medium.
 // Rounding differs from the reference's direct sums (the exact kernel is
 // bit-identical).
 //
