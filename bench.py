@@ -29,8 +29,9 @@ absorbing layers and halos: an 872 x 872 x 616 medium box), each shot a
 crop of U(192, 320) x U(192, 320) x 256 interior cells around its source
 (sources on an 8 x 8 surface grid with seeded jitter, depth 20, Ricker peak
 U(15, 25) Hz), a 48-cell sponge per shot, FP16 medium storage, 64 receivers
-per shot; tile rows and z-split chosen by the library's autotuner.  One step
-advances every shot (one persistent launch); K defaults to 1000 steps.
+per shot; tile rows, z-split and grid (persistent CTAs or one CTA per tile)
+chosen by the library's autotuner.  One step advances every shot (one
+launch); K defaults to 1000 steps.
 ``value`` is shot-point-updates per second summed over the shots.
 
 Learned form (--form learned): a 384^3 interior with the 8-cell learned
@@ -564,6 +565,7 @@ def run_batched(args, rank, world, local):
         (ty, zsplit), tune_ms = b.tiles(), None
     else:
         ty, zsplit, tune_ms = b.autotune(3)
+    persistent = b.persistent
     pts = b.points
     b.run(args.warmup)
     b.synchronize()
@@ -611,12 +613,13 @@ def run_batched(args, rank, world, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded 12-layer TTI medium, numpy PCG64 seed 2026, generated on "
                 "GPU; shot layout PCG64 seed 2027)",
-        "config": {"workload": f"batched: {args.shots} shots in one persistent launch per step "
+        "config": {"workload": f"batched: {args.shots} shots in one launch per step "
                                f"over a shared {model[0]}x{model[1]}x"
                                f"{model[2]} medium, crops U(192,320)^2 x {BATCH_DEPTH} "
                                f"+ {ABSORB}-cell sponge, dt 0.8 ms, 15-25 Hz Ricker",
                    "form": "batched", "medium_storage": storage, "shots": args.shots,
                    "points_per_step": pts, "tiles": {"ty": ty, "zsplit": zsplit,
+                                                     "persistent": persistent,
                                                      "autotune_ms_per_step": tune_ms},
                    "global_batch": args.shots * world, "seq_len": None,
                    "parallelism": f"shots{args.shots}x{world}",
@@ -754,6 +757,7 @@ def run_best(args, rank, world, local):
         b.add_shot(sh["sizes"], sh["origin"], sh["src"], sh["fcut"], 0, 0.0)
         b.set_receivers(k, sh["rec"])
     ty, zsplit, _ = b.autotune(3)
+    persistent = b.persistent
     b.set_learned_layer(mlp, layer)
     b.run(args.warmup)
     b.synchronize()
@@ -797,7 +801,7 @@ def run_best(args, rank, world, local):
                                f"{ABSORB}-cell sponge one shot at a time",
                    "form": "best", "value_counts": "interior shot-point-updates",
                    "shots": args.shots, "interior_points_per_step": interior,
-                   "tiles": {"ty": ty, "zsplit": zsplit},
+                   "tiles": {"ty": ty, "zsplit": zsplit, "persistent": persistent},
                    "plain": {"interior_gupd_s": plain, "shots_timed": n_plain,
                              "ms_per_step": plain_ms / args.steps / n_plain},
                    "speedup_vs_plain": best / plain,

@@ -188,6 +188,8 @@ SIGNATURES = [
     ("dc_gb300_batch_set_learned_layer", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     ("dc_gb300_batch_set_tiles", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("dc_gb300_batch_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("dc_gb300_batch_set_grid", C.c_int, [C.c_void_p, C.c_int]),
+    ("dc_gb300_batch_grid", C.c_int, [C.c_void_p]),
     ("dc_gb300_batch_autotune", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int),
                                           C.POINTER(C.c_int), _fp]),
     ("dc_gb300_batch_run", C.c_int, [C.c_void_p, C.c_int]),
@@ -644,6 +646,13 @@ class Batch:
         ty, zs = C.c_int(), C.c_int()
         check(lib().dc_gb300_batch_tiles(self.h, C.byref(ty), C.byref(zs)))
         return ty.value, zs.value
+
+    def set_grid(self, persistent: bool) -> None:
+        check(lib().dc_gb300_batch_set_grid(self.h, 1 if persistent else 0))
+
+    @property
+    def persistent(self) -> bool:
+        return lib().dc_gb300_batch_grid(self.h) == 1
 
     def autotune(self, steps: int = 4):
         """(ty, zsplit, ms per step) of the fastest tile candidate; leaves

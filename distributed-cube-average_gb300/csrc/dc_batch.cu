@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -65,6 +66,7 @@ struct Batch {
   int blocks = 0;
   bool prepared = false;
   int ty = 8, zsplit = 1;
+  bool persistent = true;  // persistent CTAs, or one CTA per work item
   int steps_done = 0;
   int src_applied_step = -1;
   long launches = 0;
@@ -164,7 +166,7 @@ int refresh_narrow(Batch *b) {
 
 // Builds the device tables and the launch parameters for tile rows `ty`
 // and `zsplit` z-chunks per column.
-int prepare(Batch *b, int ty, int zsplit) {
+int prepare(Batch *b, int ty, int zsplit, bool persistent) {
   if (!b->medium_set) return fail(DC_GB300_ERR_STATE, "batch medium not set");
   if (b->shots.empty()) return fail(DC_GB300_ERR_STATE, "batch has no shots");
   int rc = refresh_narrow(b);
@@ -172,6 +174,7 @@ int prepare(Batch *b, int ty, int zsplit) {
   free_tables(b);
   b->ty = ty;
   b->zsplit = zsplit;
+  b->persistent = persistent;
   const int n = static_cast<int>(b->shots.size());
   std::string err;
   CUtensorMap tm_c[3];
@@ -310,6 +313,7 @@ int prepare(Batch *b, int ty, int zsplit) {
   int sms = 0;
   BATCH_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
   b->blocks = static_cast<int>(std::min<long long>(max_items, static_cast<long long>(sms) * per_sm));
+  if (!b->persistent) b->blocks = static_cast<int>(max_items);  // one CTA per work item
   BATCH_TRY(cudaStreamSynchronize(b->stream));
   b->prepared = true;
   return DC_GB300_OK;
@@ -371,7 +375,7 @@ int check_err(Batch *b) {
 // steps, then single launches.
 int run_steps(Batch *b, int steps) {
   if (!b->prepared) {
-    const int rc = prepare(b, b->ty, b->zsplit);
+    const int rc = prepare(b, b->ty, b->zsplit, b->persistent);
     if (rc != DC_GB300_OK) return rc;
   }
   if (b->steps_done + steps > b->max_steps)
@@ -739,6 +743,7 @@ extern "C" int dc_gb300_batch_autotune(dc_gb300_batch *h, int steps, int *ty_out
   const int tys[2] = {8, 16};
   const int splits[4] = {1, 2, 4, 8};
   int best_ty = b->ty, best_split = b->zsplit;
+  bool best_persistent = b->persistent;
   float best = -1.0f;
   cudaEvent_t e0, e1;
   BATCH_TRY(cudaEventCreate(&e0));
@@ -746,7 +751,8 @@ extern "C" int dc_gb300_batch_autotune(dc_gb300_batch *h, int steps, int *ty_out
   int rc = DC_GB300_OK;
   for (int t : tys) {
     for (int zs : splits) {
-      rc = dcg::prepare(b, t, zs);
+     for (int pers = 1; pers >= 0; --pers) {
+      rc = dcg::prepare(b, t, zs, pers != 0);
       if (rc != DC_GB300_OK) break;
       rc = dcg::reset_state(b);
       if (rc != DC_GB300_OK) break;
@@ -769,14 +775,17 @@ extern "C" int dc_gb300_batch_autotune(dc_gb300_batch *h, int steps, int *ty_out
         best = ms;
         best_ty = t;
         best_split = zs;
+        best_persistent = pers != 0;
       }
+     }
+     if (rc != DC_GB300_OK) break;
     }
     if (rc != DC_GB300_OK) break;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc != DC_GB300_OK) return rc;
-  rc = dcg::prepare(b, best_ty, best_split);
+  rc = dcg::prepare(b, best_ty, best_split, best_persistent);
   if (rc != DC_GB300_OK) return rc;
   rc = dcg::reset_state(b);
   if (rc != DC_GB300_OK) return rc;
@@ -879,6 +888,20 @@ extern "C" long long dc_gb300_batch_points(const dc_gb300_batch *h) {
   long long n = 0;
   for (const auto &s : h->impl.shots) n += (s.cfg.sx - 8) * (s.cfg.sy - 8) * (s.cfg.sz - 8);
   return n;
+}
+
+extern "C" int dc_gb300_batch_set_grid(dc_gb300_batch *h, int persistent) {
+  Batch *b = dcg::impl(h);
+  if (!b) return fail(DC_GB300_ERR_ARG, "null batch");
+  BATCH_TRY(cudaSetDevice(b->device));
+  b->persistent = persistent != 0;
+  b->prepared = false;
+  dcg::drop_graphs(b);
+  return DC_GB300_OK;
+}
+
+extern "C" int dc_gb300_batch_grid(const dc_gb300_batch *h) {
+  return h ? (h->impl.persistent ? 1 : 0) : -1;
 }
 
 extern "C" int dc_gb300_batch_tiles(const dc_gb300_batch *h, int *ty, int *zsplit) {

@@ -80,15 +80,28 @@ __device__ __forceinline__ float tanh_hw(float x) {
   return y;
 }
 
+// u = a (c0 + c0 c1 a^2); gelu = h + h tanh(u), h = a / 2.  The scalar and
+// the packed (two values, FFMA2/FMUL2) forms round identically.
+constexpr float kGeluC01 = kGeluC0 * kGeluC1;
+
 __device__ __forceinline__ float gelu(float a) {
-  const float u = kGeluC0 * fmaf(kGeluC1 * a * a, a, a);
+  const float u = fmaf(a * a, kGeluC01, kGeluC0) * a;
   const float h = 0.5f * a;
   return fmaf(h, tanh_hw(u), h);
 }
 
+__device__ __forceinline__ float2 gelu2(float2 a) {
+  const float2 t = __ffma2_rn(__fmul2_rn(a, a), make_float2(kGeluC01, kGeluC01),
+                              make_float2(kGeluC0, kGeluC0));
+  const float2 u = __fmul2_rn(t, a);
+  const float2 th = make_float2(tanh_hw(u.x), tanh_hw(u.y));
+  const float2 h = __fmul2_rn(a, make_float2(0.5f, 0.5f));
+  return __ffma2_rn(h, th, h);
+}
+
 __device__ __forceinline__ float gelu_grad(float a) {
   const float a2 = a * a;
-  const float th = tanh_hw(kGeluC0 * fmaf(kGeluC1 * a2, a, a));
+  const float th = tanh_hw(fmaf(a2, kGeluC01, kGeluC0) * a);
   const float du = kGeluC0 * fmaf(3.0f * kGeluC1, a2, 1.0f);
   return 0.5f * (1.0f + th) + 0.5f * a * (1.0f - th * th) * du;
 }
@@ -358,6 +371,21 @@ __device__ __forceinline__ void mma_bf16(float d[4], const uint32_t a[4], uint32
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// GELU of a layer's accumulator fragments, packed into the next layer's A
+// fragments (k-chunk kk = n-tiles 2kk and 2kk+1).
+__device__ __forceinline__ void gelu_to_a(const float acc[4][4], uint32_t a[2][4]) {
+#pragma unroll
+  for (int kk = 0; kk < 2; ++kk) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const float2 g0 = gelu2(make_float2(acc[2 * kk + h][0], acc[2 * kk + h][1]));
+      const float2 g1 = gelu2(make_float2(acc[2 * kk + h][2], acc[2 * kk + h][3]));
+      a[kk][2 * h] = pack_bf16(g0.x, g0.y);
+      a[kk][2 * h + 1] = pack_bf16(g1.x, g1.y);
+    }
+  }
+}
+
 // Feature sources: load(r, t, f) fills f = {p1[2t], p1[2t+1], q1[2t],
 // q1[2t+1], p0[2t], p0[2t+1], q0[2t], q0[2t+1]} of cell / sample r (p1, q1
 // at t+1, p0, q0 at t) and returns its depth.
@@ -515,13 +543,7 @@ __global__ void __launch_bounds__(128) lb_tc_kernel(const float *__restrict__ wc
       mma_bf16(acc[nt], a[0], w1[0][nt][0], w1[0][nt][1]);
       mma_bf16(acc[nt], a[1], w1[1][nt][0], w1[1][nt][1]);
     }
-#pragma unroll
-    for (int kk = 0; kk < 2; ++kk) {
-      a[kk][0] = pack_bf16(gelu(acc[2 * kk][0]), gelu(acc[2 * kk][1]));
-      a[kk][1] = pack_bf16(gelu(acc[2 * kk][2]), gelu(acc[2 * kk][3]));
-      a[kk][2] = pack_bf16(gelu(acc[2 * kk + 1][0]), gelu(acc[2 * kk + 1][1]));
-      a[kk][3] = pack_bf16(gelu(acc[2 * kk + 1][2]), gelu(acc[2 * kk + 1][3]));
-    }
+    gelu_to_a(acc, a);
     // layer 2
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt) {
@@ -531,13 +553,7 @@ __global__ void __launch_bounds__(128) lb_tc_kernel(const float *__restrict__ wc
       mma_bf16(acc[nt], a[0], w2[0][nt][0], w2[0][nt][1]);
       mma_bf16(acc[nt], a[1], w2[1][nt][0], w2[1][nt][1]);
     }
-#pragma unroll
-    for (int kk = 0; kk < 2; ++kk) {
-      a[kk][0] = pack_bf16(gelu(acc[2 * kk][0]), gelu(acc[2 * kk][1]));
-      a[kk][1] = pack_bf16(gelu(acc[2 * kk][2]), gelu(acc[2 * kk][3]));
-      a[kk][2] = pack_bf16(gelu(acc[2 * kk + 1][0]), gelu(acc[2 * kk + 1][1]));
-      a[kk][3] = pack_bf16(gelu(acc[2 * kk + 1][2]), gelu(acc[2 * kk + 1][3]));
-    }
+    gelu_to_a(acc, a);
     // layer 3: outputs in columns 0 and 1, held by the lanes with t == 0
     float y[4];
     y[0] = y[2] = t == 0 ? sb3[0] : 0.f;

@@ -406,9 +406,16 @@ int dc_gb300_batch_set_learned_layer(dc_gb300_batch *batch, const struct dc_gb30
 /* Tile rows (8 or 16) and z-chunks per column (1..64). */
 int dc_gb300_batch_set_tiles(dc_gb300_batch *batch, int ty, int zsplit);
 int dc_gb300_batch_tiles(const dc_gb300_batch *batch, int *ty, int *zsplit);
-/* Times every tile candidate for `steps` steps on this batch, keeps the
- * fastest (ms per step in *ms) and returns the batch to step 0 with zero
- * wavefields and traces: call it before the first run. */
+/* Grid of the batch kernel: persistent CTAs striding over the work items
+ * (1, the default) or one CTA per work item (0).  dc_gb300_batch_grid
+ * returns the current choice. */
+int dc_gb300_batch_set_grid(dc_gb300_batch *batch, int persistent);
+int dc_gb300_batch_grid(const dc_gb300_batch *batch);
+/* Times every candidate -- tile rows x z-split x grid (persistent or one
+ * CTA per work item) -- for `steps` steps on this batch, keeps the fastest
+ * (ms per step in *ms; the grid choice via dc_gb300_batch_grid) and returns
+ * the batch to step 0 with zero wavefields and traces: call it before the
+ * first run. */
 int dc_gb300_batch_autotune(dc_gb300_batch *batch, int steps, int *ty, int *zsplit, float *ms);
 /* Queues `steps` steps of every shot (asynchronous on the batch's stream). */
 int dc_gb300_batch_run(dc_gb300_batch *batch, int steps);

@@ -67,7 +67,8 @@ def sponge(dc, sizes):
     return out
 
 
-def run_batch(dc, coef, steps_split=(40, 30), tiles=None, form=None, shots=SHOTS):
+def run_batch(dc, coef, steps_split=(40, 30), tiles=None, form=None, shots=SHOTS,
+              persistent=True):
     form = dc.MEDIUM_PRECOMP if form is None else form
     with dc.Batch(MEDIUM, D, DT, medium=form, device=0, max_steps=STEPS + 2) as b:
         b.set_precomp(coef)
@@ -76,6 +77,7 @@ def run_batch(dc, coef, steps_split=(40, 30), tiles=None, form=None, shots=SHOTS
             b.set_receivers(i, receivers(sizes, src))
         if tiles:
             b.set_tiles(*tiles)
+        b.set_grid(persistent)
         for n in steps_split:
             b.run(n)
         b.synchronize()
@@ -113,8 +115,10 @@ def test_batch_shot_bit_identical_to_single_simulation(dc, medium_coef, batch_f3
     assert np.abs(got["pc"]).max() > 0
 
 
-def test_batch_tiles_do_not_change_results(dc, medium_coef, batch_f32):
-    other = run_batch(dc, medium_coef, steps_split=(STEPS,), tiles=(16, 3))
+@pytest.mark.parametrize("persistent", [True, False])
+def test_batch_tiles_do_not_change_results(dc, medium_coef, batch_f32, persistent):
+    other = run_batch(dc, medium_coef, steps_split=(STEPS,), tiles=(16, 3),
+                      persistent=persistent)
     for (a, ta), (b, tb) in zip(batch_f32, other):
         assert np.array_equal(a["pc"], b["pc"]) and np.array_equal(a["qc"], b["qc"])
         assert np.array_equal(ta, tb)
