@@ -483,7 +483,9 @@ long long dc_gb300_layer_cells(long sx, long sy, long sz, int layer, int *cells,
 /* Applies the MLP after every stencil pass of dc_gb300_run to the layer
  * cells of a layer `layer` cells wide (1..DC_GB300_MLP_DEPTHS; 0 turns it
  * off).  The simulation reads the MLP's parameters at every step: keep the
- * MLP alive while it is set. */
+ * MLP alive while it is set, and do not train it or set its parameters
+ * while a run that uses it may still be executing (the MLP and the
+ * simulation have separate streams; synchronise the simulation first). */
 int dc_gb300_set_learned_layer(dc_gb300_sim *sim, const dc_gb300_mlp *mlp, int layer);
 /* Teacher-forced training samples: the fields of `wide` (t and t-1) are
  * cropped at offset[] to the box of `thin` (zero halo), `thin` steps once
