@@ -182,8 +182,8 @@ def make_rollout_samples(setup: Setup, mlp: MLP, sources, steps: int, starts, se
         thin.close()
 
 
-def fit(setup: Setup, mlp: MLP, sources, steps: int, rounds: int = 3, train_steps: int = 2000,
-        batch: int = 8192, lr: float = 2e-3, seg: int = 12, first: int = 40, every: int = 6,
+def fit(setup: Setup, mlp: MLP, sources, steps: int, rounds: int = 6, train_steps: int = 2000,
+        batch: int = 8192, lr: float = 2e-3, seg: int = 16, first: int = 40, every: int = 6,
         seed: int = 1, device=0):
     """Teacher-forced samples and training, then ``rounds`` rounds of
     rollout samples from the current network added to the same set
@@ -206,7 +206,7 @@ def fit(setup: Setup, mlp: MLP, sources, steps: int, rounds: int = 3, train_step
     return np.concatenate(hist)
 
 
-def select(setup: Setup, seeds, sources, val_sources, steps: int, rounds: int = 3,
+def select(setup: Setup, seeds, sources, val_sources, steps: int, rounds: int = 6,
            band: int = 12, every: int = 20, device=0, **fit_args):
     """Trains one network per seed and keeps the one with the lowest
     reflected energy on the validation shots.  Returns (mlp or None,
@@ -339,13 +339,14 @@ def main(argv=None):
     ap = argparse.ArgumentParser(prog="learned")
     ap.add_argument("--out", default=str(WEIGHTS))
     ap.add_argument("--seeds", type=int, nargs="+", default=[11, 12, 13, 14])
-    ap.add_argument("--rounds", type=int, default=4)
+    ap.add_argument("--rounds", type=int, default=6)
+    ap.add_argument("--seg", type=int, default=16)
     ap.add_argument("--n", type=int, default=48)
     ap.add_argument("--steps", type=int, default=320)
     args = ap.parse_args(argv)
     st = Setup(n=(args.n,) * 3, layer=8)
     mlp, report = select(st, args.seeds, random_sources(st, 4, 7), random_sources(st, 2, 55),
-                         steps=args.steps, rounds=args.rounds)
+                         steps=args.steps, rounds=args.rounds, seg=args.seg)
     if mlp is None:
         raise SystemExit("no network beat the thin layer without it")
     np.save(args.out, mlp.params())

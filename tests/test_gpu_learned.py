@@ -128,7 +128,7 @@ def test_trained_layer_reduces_reflections(dc, torch):
     from dc_gb300 import learned as L
     st = L.Setup(n=(48, 48, 48), layer=8)
     mlp, report = L.select(st, [11, 12, 13], L.random_sources(st, 4, 7),
-                           L.random_sources(st, 2, 55), steps=320, rounds=4)
+                           L.random_sources(st, 2, 55), steps=320)
     print("selection:", report)
     assert mlp is not None
     with mlp:
