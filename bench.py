@@ -136,6 +136,23 @@ def parse():
     return args
 
 
+def max_over_ranks(v: float, dist, device: str) -> float:
+    """Largest value over the ranks (the slowest rank's time); v itself when
+    running alone."""
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def weak_rate(points_per_step: int, steps: int, world: int, ms: float) -> float:
+    """Whole-job rate in G updates/s: every one of the `world` ranks updated
+    points_per_step points `steps` times in `ms` (the max over ranks)."""
+    return points_per_step * steps * world / (ms * 1e-3) / 1e9
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -341,12 +358,8 @@ def run_ours(args, rank, world, local):
         if dist is not None:
             dist.barrier()
 
-    def max_over_ranks(v: float) -> float:
-        if dist is None:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    def max_ms(v: float) -> float:
+        return max_over_ranks(v, dist, "cuda")
 
     geom = geometry(args.nxyz)
     sizes = geom.sizes
@@ -382,9 +395,9 @@ def run_ours(args, rank, world, local):
     sim.synchronize()
     launches = sim.launches - l0
     ms = ev0.elapsed_time(ev1)
-    ms = max_over_ranks(ms)
+    ms = max_ms(ms)
     barrier()
-    value = pts * args.steps * world / (ms * 1e-3) / 1e9
+    value = weak_rate(pts, args.steps, world, ms)
     stencil_ms = ms / args.steps  # graph-replayed region: one stencil launch per step
     achieved = bytes_per_update * pts / (stencil_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
@@ -396,8 +409,7 @@ def run_ours(args, rank, world, local):
     # ---- end to end through the reference ABI with host buffers ----------
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_over_ranks,
-                      world)
+        e2e = run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_ms, world)
 
     # ---- CPU baseline: the oracle on a slab (rank 0, N = 1) ---------------
     cpu = None
@@ -443,7 +455,7 @@ def run_ours(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
-def run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_over_ranks, world):
+def run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_ms, world):
     """Same workload through the reference's entry points with host
     buffers: the medium comes from pinned host arrays, the loop is
     src/worker.c's (source, propagate, swap), results come back to the
@@ -498,7 +510,7 @@ def run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_over_ran
     dc.device_data_get_results(proc, data)
     el = time.perf_counter() - t0
     dc.device_data_free(data)
-    el = max_over_ranks(el)
+    el = max_ms(el)
     h2d = 14 * sx * sy * sz * 4
     d2h = 2 * sx * sy * sz * 4
     return {"value": pts * args.steps * world / el / 1e9, "unit": UNIT,
@@ -582,15 +594,11 @@ def run_batched(args, rank, world, local):
         torch.cuda.synchronize()
     b.synchronize()
     launches = b.launches - l0
-    ms = ev0.elapsed_time(ev1)
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
     tr = b.traces(0, total)
     assert np.isfinite(tr).all()
     b.close()
-    value = pts * args.steps * world / (ms * 1e-3) / 1e9
+    value = weak_rate(pts, args.steps, world, ms)
     bytes_per_update = 44 if storage in ("f16", "bf16") else 64
     achieved = bytes_per_update * pts / (ms / args.steps * 1e-3) / 1e9
     peak, peak_kind = peaks()
