@@ -458,31 +458,38 @@ struct BatchCellSrc {  // the layer cells of every shot of a batch
   }
 };
 
+// The weights' B fragments live in shared memory (one 8-byte entry per
+// lane and 16 x 8 block, read with one LDS.64 per MMA), which keeps the
+// kernel under 64 registers: eight 4-warp CTAs per SM hide the gathers'
+// latency.
 template <class Src>
-__global__ void __launch_bounds__(128) lb_tc_kernel(const float *__restrict__ wc, Src src,
-                                                    long long n, float2 *out) {
+__global__ void __launch_bounds__(128, 8) lb_tc_kernel(const float *__restrict__ wc, Src src,
+                                                       long long n, float2 *out) {
   __shared__ float sb1[kDepths * kHid], sb2[kHid], sb3[kOut];
+  __shared__ uint2 bw1[2][4][32], bw2[2][4][32], bw3[2][32];
   for (int i = threadIdx.x; i < kDepths * kHid; i += blockDim.x) sb1[i] = wc[OFF_B1 + i];
   if (threadIdx.x < kHid) sb2[threadIdx.x] = wc[OFF_B2 + threadIdx.x];
   if (threadIdx.x < kOut) sb3[threadIdx.x] = wc[OFF_B3 + threadIdx.x];
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  // B fragments: B[k][n] = W[n][k] of each 16 x 8 (k x n) block
-  uint32_t w1[2][4][2], w2[2][4][2], w3[2][2];
+  if (threadIdx.x < 32) {
+    // B fragments: B[k][n] = W[n][k] of each 16 x 8 (k x n) block
 #pragma unroll
-  for (int kk = 0; kk < 2; ++kk) {
-    const int k0 = kk * 16 + 2 * t;
+    for (int kk = 0; kk < 2; ++kk) {
+      const int k0 = kk * 16 + 2 * t;
 #pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-      const float *r1 = wc + OFF_W1 + (nt * 8 + g) * kIn;
-      const float *r2 = wc + OFF_W2 + (nt * 8 + g) * kHid;
-      w1[kk][nt][0] = pack_bf16(r1[k0], r1[k0 + 1]);
-      w1[kk][nt][1] = pack_bf16(r1[k0 + 8], r1[k0 + 9]);
-      w2[kk][nt][0] = pack_bf16(r2[k0], r2[k0 + 1]);
-      w2[kk][nt][1] = pack_bf16(r2[k0 + 8], r2[k0 + 9]);
+      for (int nt = 0; nt < 4; ++nt) {
+        const float *r1 = wc + OFF_W1 + (nt * 8 + g) * kIn;
+        const float *r2 = wc + OFF_W2 + (nt * 8 + g) * kHid;
+        bw1[kk][nt][lane] = make_uint2(pack_bf16(r1[k0], r1[k0 + 1]),
+                                       pack_bf16(r1[k0 + 8], r1[k0 + 9]));
+        bw2[kk][nt][lane] = make_uint2(pack_bf16(r2[k0], r2[k0 + 1]),
+                                       pack_bf16(r2[k0 + 8], r2[k0 + 9]));
+      }
+      const float *r3 = wc + OFF_W3 + min(g, kOut - 1) * kHid;
+      bw3[kk][lane] = g < kOut ? make_uint2(pack_bf16(r3[k0], r3[k0 + 1]),
+                                            pack_bf16(r3[k0 + 8], r3[k0 + 9]))
+                               : make_uint2(0u, 0u);
     }
-    const float *r3 = wc + OFF_W3 + min(g, kOut - 1) * kHid;
-    w3[kk][0] = g < kOut ? pack_bf16(r3[k0], r3[k0 + 1]) : 0u;
-    w3[kk][1] = g < kOut ? pack_bf16(r3[k0 + 8], r3[k0 + 9]) : 0u;
   }
   __syncthreads();
   const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -540,8 +547,9 @@ __global__ void __launch_bounds__(128) lb_tc_kernel(const float *__restrict__ wc
       acc[nt][1] = sb1[d0 * kHid + c + 1];
       acc[nt][2] = sb1[d1 * kHid + c];
       acc[nt][3] = sb1[d1 * kHid + c + 1];
-      mma_bf16(acc[nt], a[0], w1[0][nt][0], w1[0][nt][1]);
-      mma_bf16(acc[nt], a[1], w1[1][nt][0], w1[1][nt][1]);
+      const uint2 b0 = bw1[0][nt][lane], b1 = bw1[1][nt][lane];
+      mma_bf16(acc[nt], a[0], b0.x, b0.y);
+      mma_bf16(acc[nt], a[1], b1.x, b1.y);
     }
     gelu_to_a(acc, a);
     // layer 2
@@ -550,16 +558,20 @@ __global__ void __launch_bounds__(128) lb_tc_kernel(const float *__restrict__ wc
       const int c = nt * 8 + 2 * t;
       acc[nt][0] = acc[nt][2] = sb2[c];
       acc[nt][1] = acc[nt][3] = sb2[c + 1];
-      mma_bf16(acc[nt], a[0], w2[0][nt][0], w2[0][nt][1]);
-      mma_bf16(acc[nt], a[1], w2[1][nt][0], w2[1][nt][1]);
+      const uint2 b0 = bw2[0][nt][lane], b1 = bw2[1][nt][lane];
+      mma_bf16(acc[nt], a[0], b0.x, b0.y);
+      mma_bf16(acc[nt], a[1], b1.x, b1.y);
     }
     gelu_to_a(acc, a);
     // layer 3: outputs in columns 0 and 1, held by the lanes with t == 0
     float y[4];
     y[0] = y[2] = t == 0 ? sb3[0] : 0.f;
     y[1] = y[3] = t == 0 ? sb3[1] : 0.f;
-    mma_bf16(y, a[0], w3[0][0], w3[0][1]);
-    mma_bf16(y, a[1], w3[1][0], w3[1][1]);
+    {
+      const uint2 b0 = bw3[0][lane], b1 = bw3[1][lane];
+      mma_bf16(y, a[0], b0.x, b0.y);
+      mma_bf16(y, a[1], b1.x, b1.y);
+    }
     if (t == 0) {
       if (r0 < n) out[r0] = make_float2(rr0 * y[0], rr0 * y[1]);
       if (r1 < n) out[r1] = make_float2(rr1 * y[2], rr1 * y[3]);
