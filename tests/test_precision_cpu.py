@@ -1,0 +1,44 @@
+"""Why the wavefields stay FP32 (CPU, oracle emulation): on a layered
+medium, rounding p and q to FP16 (power-of-two scale per field) or BF16 at
+every store costs far more than the 1e-3 relative-L2 budget against the
+FP64 oracle, while FP16 storage of the coefficients alone stays inside it.
+The storage rounding is emulated by the oracle's store modes (the GPU
+kernels never store narrow wavefields)."""
+import numpy as np
+
+from oracle.oracle import KIND_F32, KIND_F64, STORE_BF16, STORE_F16, Geometry, rel_l2
+
+
+def _narrow_f16(coef):
+    out = []
+    for c in coef:
+        m = float(np.abs(c).max())
+        sc = 2.0 ** (14 - int(np.floor(np.log2(m)))) if m > 0 else 1.0
+        out.append((np.asarray(c * sc, np.float32).astype(np.float16).astype(np.float32)
+                    / np.float32(sc)).astype(np.float32))
+    return out
+
+
+def test_narrow_wavefields_miss_the_accuracy_budget(dc, port):
+    from dc_gb300 import medium
+    g = Geometry((40, 40, 40), 8)
+    coef = port.precomp(medium.layered_fields(medium.layered_spec(7, g.sizes), g.sizes))
+    steps, dt = 200, 0.8e-3
+    common = dict(src_index=g.index(g.sizes[0] // 2, g.sizes[1] // 2, 4 + 8 + 10),
+                  src=port.source_table(dt, steps, 60.0),
+                  sponge=[port.sponge_profile(s, 8, 0.35) for s in g.sizes])
+    z32 = lambda: [np.zeros(g.shape, np.float32) for _ in range(4)]  # noqa: E731
+    f64 = port.run(KIND_F64, g.sizes, (12.5,) * 3, dt, steps,
+                   *[np.zeros(g.shape, np.float64) for _ in range(4)], coef=coef, **common)
+    c16 = _narrow_f16(coef)
+    coef_only = port.run(KIND_F32, g.sizes, (12.5,) * 3, dt, steps, *z32(), coef=c16, **common)
+    f16 = port.run(KIND_F32, g.sizes, (12.5,) * 3, dt, steps, *z32(), coef=c16, store=STORE_F16,
+                   store_exp=(10, 10), **common)
+    bf16 = port.run(KIND_F32, g.sizes, (12.5,) * 3, dt, steps, *z32(), coef=c16,
+                    store=STORE_BF16, **common)
+    e_coef = rel_l2(coef_only.pc, f64.pc)
+    e_f16, e_bf16 = rel_l2(f16.pc, f64.pc), rel_l2(bf16.pc, f64.pc)
+    print(f"rel. L2 vs FP64 after {steps} steps: FP16 coefficients {e_coef:.2e}, "
+          f"+ FP16 wavefields {e_f16:.2e}, + BF16 wavefields {e_bf16:.2e}")
+    assert e_coef < 1e-3
+    assert e_f16 > 1e-3 and e_bf16 > 1e-2
