@@ -15,22 +15,31 @@
  *     bulk writes instead of one seek + write per element;
  *   - the same CSV timing lines (src/main.c:200-215).
  * Extensions (optional): --steps, --fcut, --kernel, --loop, --boundary,
- * --sponge-kappa, --checkpoint, --resume, --print-iterations.
+ * --sponge-kappa, --learned-weights, --checkpoint, --resume,
+ * --print-iterations.  --boundary learned keeps the default medium in the
+ * absorbing zone (no random velocity boundary) and corrects its outer cells
+ * with the learned thin layer (weights: a .npy file of
+ * DC_GB300_MLP_PARAMS float32 values, by default data/learned_layer8.npy
+ * beside the executable).
  */
 #include <argp.h>
+#include <limits.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#include <unistd.h>
 
 #include "dc_gb300.h"
 
 enum {
   K_SX = 128, K_SY, K_SZ, K_DX, K_DY, K_DZ, K_DT, /* src/main.c:17-23 */
   K_STEPS = 200, K_FCUT, K_KERNEL, K_LOOP, K_BOUNDARY, K_KAPPA, K_CKPT, K_RESUME,
-  K_PRINT_IT
+  K_PRINT_IT, K_WEIGHTS
 };
+
+enum { B_RVB = 0, B_SPONGE = 1, B_LEARNED = 2 };
 
 typedef struct {
   size_t size_x, size_y, size_z;
@@ -41,8 +50,9 @@ typedef struct {
   double fcut;
   int kernel;         /* DC_GB300_KERNEL_* */
   int loop_abi;       /* 1: the reference ABI loop, 0: dc_gb300_run */
-  int sponge;         /* 0: random velocity boundary only, 1: + sponge */
+  int boundary;       /* B_RVB, B_SPONGE (random velocity boundary + sponge), B_LEARNED */
   double kappa;
+  char *weights;
   char *checkpoint, *resume;
   int print_iterations;
 } cli_args;
@@ -62,8 +72,9 @@ static struct argp_option options[] = {
     {"fcut", K_FCUT, "FLOAT", 0, "Source cut-off frequency (default 40; peak = fcut/3)"},
     {"kernel", K_KERNEL, "fast|exact", 0, "Stencil arithmetic (default fast)"},
     {"loop", K_LOOP, "graph|abi", 0, "Time loop: graph-captured runs (default) or the reference ABI calls"},
-    {"boundary", K_BOUNDARY, "rvb|sponge", 0, "Absorbing boundary (default rvb)"},
+    {"boundary", K_BOUNDARY, "rvb|sponge|learned", 0, "Absorbing boundary (default rvb)"},
     {"sponge-kappa", K_KAPPA, "FLOAT", 0, "Sponge strength (default 0.35)"},
+    {"learned-weights", K_WEIGHTS, "PATH", 0, "Network of --boundary learned (.npy)"},
     {"checkpoint", K_CKPT, "PATH", 0, "Write a checkpoint after the run"},
     {"resume", K_RESUME, "PATH", 0, "Resume from a checkpoint"},
     {"print-iterations", K_PRINT_IT, 0, 0, "Print the iteration count and exit"},
@@ -95,10 +106,12 @@ static error_t parse_opt(int key, char *arg, struct argp_state *state) {
     else argp_error(state, "--loop must be graph or abi");
     break;
   case K_BOUNDARY:
-    if (strcmp(arg, "sponge") == 0) a->sponge = 1;
-    else if (strcmp(arg, "rvb") == 0) a->sponge = 0;
-    else argp_error(state, "--boundary must be rvb or sponge");
+    if (strcmp(arg, "sponge") == 0) a->boundary = B_SPONGE;
+    else if (strcmp(arg, "rvb") == 0) a->boundary = B_RVB;
+    else if (strcmp(arg, "learned") == 0) a->boundary = B_LEARNED;
+    else argp_error(state, "--boundary must be rvb, sponge or learned");
     break;
+  case K_WEIGHTS: a->weights = strdup(arg); break;
   case K_KAPPA: a->kappa = atof(arg); break;
   case K_CKPT: a->checkpoint = strdup(arg); break;
   case K_RESUME: a->resume = strdup(arg); break;
@@ -118,6 +131,39 @@ static error_t parse_opt(int key, char *arg, struct argp_state *state) {
 
 static struct argp argp_def = {options, parse_opt, NULL,
                                "Fletcher TTI propagation on one GB300 (dc_gb300)"};
+
+/* Reads a .npy file holding exactly `count` little-endian float32 values
+ * (format versions 1 and 2, C order). */
+static int read_npy_f32(const char *path, float *out, size_t count) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return -1;
+  unsigned char head[10];
+  int ok = fread(head, 1, 8, f) == 8 && memcmp(head, "\x93NUMPY", 6) == 0;
+  unsigned long hlen = 0;
+  if (ok && head[6] == 1) {
+    unsigned char b[2];
+    ok = fread(b, 1, 2, f) == 2;
+    hlen = b[0] | (unsigned long)b[1] << 8;
+  } else if (ok && (head[6] == 2 || head[6] == 3)) {
+    unsigned char b[4];
+    ok = fread(b, 1, 4, f) == 4;
+    hlen = b[0] | (unsigned long)b[1] << 8 | (unsigned long)b[2] << 16 | (unsigned long)b[3] << 24;
+  } else {
+    ok = 0;
+  }
+  char *hdr = ok && hlen < 65536 ? (char *)malloc(hlen + 1) : NULL;
+  ok = ok && hdr && fread(hdr, 1, hlen, f) == hlen;
+  if (ok) {
+    hdr[hlen] = 0;
+    char shape[64];
+    snprintf(shape, sizeof(shape), "(%zu,)", count);
+    ok = strstr(hdr, "'<f4'") && strstr(hdr, "'fortran_order': False") && strstr(hdr, shape);
+  }
+  free(hdr);
+  ok = ok && fread(out, sizeof(float), count, f) == count;
+  fclose(f);
+  return ok ? 0 : -1;
+}
 
 static double now_s(void) {
   struct timespec ts;
@@ -182,9 +228,10 @@ int main(int argc, char **argv) {
   /* medium: src/main.c:158-172 for the one rank at the origin */
   dc_anisotropy_t aniso = dc_compute_anisotropy_vars((int)sx, (int)sy, (int)sz);
   unsigned int seed = 0;
-  randomVelocityBoundaryPartition((int)sx, (int)sy, (int)sz, (int)sx, (int)sy, (int)sz, 0, 0, 0,
-                                  (int)a.size_x, (int)a.size_y, (int)a.size_z, 4,
-                                  (int)a.absorption, aniso.vpz, aniso.vsv, &seed);
+  if (a.boundary != B_LEARNED) /* the learned layer absorbs in the default medium */
+    randomVelocityBoundaryPartition((int)sx, (int)sy, (int)sz, (int)sx, (int)sy, (int)sz, 0, 0,
+                                    0, (int)a.size_x, (int)a.size_y, (int)a.size_z, 4,
+                                    (int)a.absorption, aniso.vpz, aniso.vsv, &seed);
   dc_precomp_vars pre = dc_compute_precomp_vars((int)sx, (int)sy, (int)sz, aniso);
   float *pc = (float *)calloc(n, sizeof(float));
   float *qc = (float *)calloc(n, sizeof(float));
@@ -199,8 +246,10 @@ int main(int argc, char **argv) {
   double loop_t0 = 0, loop_t1 = 0;
   if (a.loop_abi) {
     /* src/worker.c:451-525 through the reference ABI, one box per step */
-    if (a.sponge || a.checkpoint || a.resume) {
-      fprintf(stderr, "[dc_gb300] --loop abi supports neither the sponge nor checkpoints\n");
+    if (a.boundary != B_RVB || a.checkpoint || a.resume) {
+      fprintf(stderr,
+              "[dc_gb300] --loop abi supports neither the sponge, the learned layer nor "
+              "checkpoints\n");
       return 1;
     }
     if (a.kernel == DC_GB300_KERNEL_EXACT) setenv("DC_GB300_KERNEL", "exact", 1);
@@ -255,7 +304,30 @@ int main(int argc, char **argv) {
     /* after set_source: the checkpoint records whether pc holds the next
        step's source already */
     if (a.resume && dc_gb300_load_checkpoint(sim, a.resume) != DC_GB300_OK) die("resume");
-    if (a.sponge) {
+    dc_gb300_mlp *mlp = NULL;
+    if (a.boundary == B_LEARNED) {
+      char def[PATH_MAX];
+      const char *wpath = a.weights;
+      if (!wpath) { /* data/learned_layer8.npy beside the executable */
+        const ssize_t len = readlink("/proc/self/exe", def, sizeof(def) - 40);
+        if (len <= 0) die("locate the executable");
+        def[len] = 0;
+        char *slash = strrchr(def, '/');
+        strcpy(slash ? slash + 1 : def, "data/learned_layer8.npy");
+        wpath = def;
+      }
+      float *w = (float *)malloc(sizeof(float) * DC_GB300_MLP_PARAMS);
+      if (!w || read_npy_f32(wpath, w, DC_GB300_MLP_PARAMS) != 0) {
+        fprintf(stderr, "[dc_gb300] cannot read network weights from %s\n", wpath);
+        return 1;
+      }
+      if (dc_gb300_mlp_create(cfg.device, &mlp) != DC_GB300_OK) die("mlp_create");
+      if (dc_gb300_mlp_set_params(mlp, w) != DC_GB300_OK) die("mlp_set_params");
+      free(w);
+      if (dc_gb300_set_learned_layer(sim, mlp, (int)a.absorption) != DC_GB300_OK)
+        die("set_learned_layer");
+    }
+    if (a.boundary == B_SPONGE) {
       float *g[3];
       const size_t s3[3] = {sx, sy, sz};
       for (int d = 0; d < 3; ++d) {
@@ -275,6 +347,7 @@ int main(int argc, char **argv) {
     if (a.checkpoint && dc_gb300_save_checkpoint(sim, a.checkpoint) != DC_GB300_OK)
       die("checkpoint");
     dc_gb300_destroy(sim);
+    dc_gb300_mlp_destroy(mlp);
   }
   const double total = now_s() - t0;
   if (a.output_file && write_results(a.output_file, pc, qc, sx, sy, sz) != 0) {
@@ -294,5 +367,6 @@ int main(int argc, char **argv) {
   free(qc);
   free(amp);
   free(a.output_file);
+  free(a.weights);
   return 0;
 }

@@ -134,3 +134,33 @@ def test_checkpoint_api_roundtrip(dc, port, tmp_path):
     with dc.Simulation((16, 16, 16), (12.5,) * 3, 1e-3, device=0) as c:
         with pytest.raises(dc.DcError):
             c.load_checkpoint(ck)  # other sizes
+
+
+@pytest.mark.gpu
+def test_cli_learned_boundary(dc, port, tmp_path):
+    """--boundary learned: the default medium (no random velocity boundary)
+    with the committed network on an 8-cell layer gives exactly what a
+    simulation with the same layer gives; a bad weights file is refused."""
+    from dc_gb300 import learned
+    n, absorb, dt, steps = (20, 18, 16), 8, 1e-3, 60
+    out = tmp_path / "out.dc"
+    args = ["--size-x", n[0], "--size-y", n[1], "--size-z", n[2], *BASE, "--dt", dt,
+            "-t", 1.0, "-a", absorb, "--steps", steps, "--boundary", "learned"]
+    cli(dc, *args, "-o", out)
+    geom = Geometry(n, absorb)
+    coef = port.precomp(port.default_anisotropy(geom.shape))
+    with dc.MLP(device=0, params=np.load(learned.WEIGHTS)) as mlp:
+        with dc.Simulation(geom.sizes, (12.5,) * 3, dt, kernel=dc.KERNEL_FAST, device=0) as sim:
+            sim.set_precomp(coef)
+            sim.set_fields()
+            sim.set_source(geom.source_index, dc.source_table(dt, steps + 1, 40.0))
+            dc.set_learned_layer(sim, mlp, absorb)
+            sim.run(steps)
+            sim.synchronize()
+            want = sim.get_fields()
+    pc, qc = read_output(out, geom)
+    assert np.array_equal(pc, want["pc"]) and np.array_equal(qc, want["qc"])
+    bad = tmp_path / "bad.npy"
+    np.save(bad, np.zeros(10, np.float32))
+    r = cli(dc, *args, "-o", tmp_path / "x.dc", "--learned-weights", bad, check=False)
+    assert r.returncode != 0 and "weights" in r.stderr
