@@ -46,6 +46,7 @@ class Setup:
     dt: float = 0.8e-3
     fcut: float = 60.0
     seed: int = 2026              # medium seed
+    medium_args: tuple = ()       # extra layered_spec arguments, as (name, value) pairs
 
     @property
     def thin_sizes(self):
@@ -69,7 +70,7 @@ class Setup:
         return tuple(v + 2 * self.sponge_absorb + 8 for v in self.n)
 
     def spec(self):
-        return _medium.layered_spec(self.seed, self.wide_sizes)
+        return _medium.layered_spec(self.seed, self.wide_sizes, **dict(self.medium_args))
 
 
 def _origin_spec(setup: Setup, origin):
