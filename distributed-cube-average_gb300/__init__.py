@@ -636,8 +636,11 @@ class Batch:
         self.nrec[shot] = int(a.shape[0])
 
     def set_learned_layer(self, mlp: "MLP | None", layer: int) -> None:
+        """Every shot reads the network at every step: the batch keeps a
+        reference to ``mlp`` for as long as the layer is set."""
         check(lib().dc_gb300_batch_set_learned_layer(self.h, mlp.h if mlp is not None else None,
                                                      int(layer)))
+        self._mlp = mlp if layer > 0 else None
 
     def set_tiles(self, ty: int, zsplit: int) -> None:
         check(lib().dc_gb300_batch_set_tiles(self.h, int(ty), int(zsplit)))
@@ -771,7 +774,10 @@ def layer_cells(sizes, layer: int) -> np.ndarray:
 
 
 def set_learned_layer(sim: "Simulation", mlp: "MLP | None", layer: int) -> None:
+    """The simulation reads the network's parameters at every step: it keeps
+    a reference to ``mlp`` for as long as the layer is set."""
     check(lib().dc_gb300_set_learned_layer(sim.h, mlp.h if mlp is not None else None, int(layer)))
+    sim._mlp = mlp if layer > 0 else None
 
 
 def lb_sample(wide: "Simulation", thin: "Simulation", offset, layer: int, samples_ptr: int,
