@@ -774,9 +774,13 @@ def run_best(args, rank, world, local):
         ms = timed_run(b, args.steps)
     launches = b.launches - l0
     assert np.isfinite(b.traces(0, total)).all()
+    compute_pts = b.points
     b.close()
     mlp.close()
     best = interior * args.steps / (ms * 1e-3) / 1e9
+    # stencil bytes (FP16 medium: 44 B per updated point) over the whole step
+    achieved = 44 * compute_pts / (ms / args.steps * 1e-3) / 1e9
+    peak, peak_kind = peaks()
     # plain form: FP32, 48-cell sponge, one shot at a time, first shots
     n_plain = min(2, len(wide))
     plain_pts, plain_ms = 0, 0.0
@@ -819,7 +823,11 @@ def run_best(args, rank, world, local):
                    "global_batch": args.shots * world, "seq_len": None,
                    "parallelism": f"shots{args.shots}x{world}",
                    "l2": "inputs ~40 GB >> 129 MB L2; no flush"},
-        "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "bytes_per_update": 44,
+                     "note": "stencil bytes per updated point over the whole step "
+                             "(stencil + network + correction)", "traffic": None},
+        "cpu_baseline": None, "e2e": None, "gpu_launches": launches,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
