@@ -12,9 +12,9 @@
 // FMA contraction (and to its CUDA arithmetic executed the same way).
 //
 // Data path: a CTA owns a 32 x 4 column tile and sweeps a chunk of z.  The
-// stencil reads go through the read-only data cache; each point reads 434
-// stencil values, so this kernel is bound by L1 bandwidth, not HBM.  It is
-// the parity anchor, not the throughput path.
+// stencil reads go through the read-only data cache as (p, q) pairs (217
+// 8-byte loads per point), so this kernel is bound by L1 bandwidth, not
+// HBM.  It is the parity anchor, not the throughput path.
 #include "dc_internal.h"
 
 namespace dcg {
@@ -39,66 +39,82 @@ __device__ __forceinline__ constexpr int pair_b(int g) {
   return g < 4 ? g + 1 : g < 7 ? g - 2 : g < 9 ? g - 4 : 4;
 }
 
-__device__ __forceinline__ float der2_x(const float *__restrict__ p,
-                                        long long i, long long s, float inv) {
-  float a = __fmul_rn(kw(0), __ldg(p + i));
-  a = __fadd_rn(a, __fmul_rn(kw(1), __fadd_rn(__ldg(p + i + s), __ldg(p + i - s))));
-  a = __fadd_rn(a, __fmul_rn(kw(2), __fadd_rn(__ldg(p + i + 2 * s), __ldg(p + i - 2 * s))));
-  a = __fadd_rn(a, __fmul_rn(kw(3), __fadd_rn(__ldg(p + i + 3 * s), __ldg(p + i - 3 * s))));
-  a = __fadd_rn(a, __fmul_rn(kw(4), __fadd_rn(__ldg(p + i + 4 * s), __ldg(p + i - 4 * s))));
-  return __fmul_rn(a, inv);
-}
-
-__device__ __forceinline__ float cross_x(const float *__restrict__ p,
-                                         long long i, long long s1,
-                                         long long s2, float inv) {
-  float total = 0.0f;
-#pragma unroll
-  for (int g = 0; g < 10; ++g) {
-    const long long a = pair_a(g), b = pair_b(g);
-    float acc = __ldg(p + i + a * s2 + b * s1);
-    acc = __fsub_rn(acc, __ldg(p + i + a * s2 - b * s1));
-    acc = __fsub_rn(acc, __ldg(p + i - a * s2 + b * s1));
-    acc = __fadd_rn(acc, __ldg(p + i - a * s2 - b * s1));
-    if (a != b) {
-      acc = __fadd_rn(acc, __ldg(p + i + b * s2 + a * s1));
-      acc = __fsub_rn(acc, __ldg(p + i + b * s2 - a * s1));
-      acc = __fsub_rn(acc, __ldg(p + i - b * s2 + a * s1));
-      acc = __fadd_rn(acc, __ldg(p + i - b * s2 - a * s1));
-    }
-    const float w = static_cast<float>(lw(pair_a(g)) * lw(pair_b(g)));
-    const float term = __fmul_rn(w, acc);
-    total = g == 0 ? term : __fadd_rn(total, term);
-  }
-  return __fmul_rn(total, inv);
-}
-
 struct H12 {
   float h1, h2;
 };
 
-// `f` points at one component of a pair buffer: element strides are doubled
-// (sX = 2, sY = 2*pitch, sZ = 2*plane, i = 2*index).
-__device__ __forceinline__ H12 hterms(const float *__restrict__ f, long long i,
-                                      long long sX, long long sY, long long sZ,
-                                      const StepParams &prm, float cxx,
-                                      float cyy, float czz, float cxy,
-                                      float cyz, float cxz) {
-  const float fxx = der2_x(f, i, sX, prm.dxxinv);
-  const float fyy = der2_x(f, i, sY, prm.dyyinv);
-  const float fzz = der2_x(f, i, sZ, prm.dzzinv);
-  const float fxy = cross_x(f, i, sX, sY, prm.dxyinv);
-  const float fyz = cross_x(f, i, sY, sZ, prm.dyzinv);
-  const float fxz = cross_x(f, i, sX, sZ, prm.dxzinv);
-  float h1 = __fmul_rn(cxx, fxx);
-  h1 = __fadd_rn(h1, __fmul_rn(cyy, fyy));
-  h1 = __fadd_rn(h1, __fmul_rn(czz, fzz));
-  h1 = __fadd_rn(h1, __fmul_rn(cxy, fxy));
-  h1 = __fadd_rn(h1, __fmul_rn(cxz, fxz));
-  h1 = __fadd_rn(h1, __fmul_rn(cyz, fyz));
-  const float h2 = __fsub_rn(__fadd_rn(__fadd_rn(fxx, fyy), fzz), h1);
-  return H12{h1, h2};
+// der2 (include/derivatives.h:47-54) and derCross (:56-91) of p and q
+// together: one 8-byte load of a (p, q) pair feeds both fields, and each
+// field's arithmetic is the reference's, term by term and in its order.
+__device__ __forceinline__ float2 ldp(const float2 *__restrict__ f, long long i) {
+  return __ldg(f + i);
 }
+
+__device__ __forceinline__ float2 der2_x2(const float2 *__restrict__ f, long long i, long long s,
+                                          float inv) {
+  const float2 c = ldp(f, i);
+  float2 a = make_float2(__fmul_rn(kw(0), c.x), __fmul_rn(kw(0), c.y));
+#pragma unroll
+  for (int k = 1; k <= 4; ++k) {
+    const float2 u = ldp(f, i + k * s), v = ldp(f, i - k * s);
+    a.x = __fadd_rn(a.x, __fmul_rn(kw(k), __fadd_rn(u.x, v.x)));
+    a.y = __fadd_rn(a.y, __fmul_rn(kw(k), __fadd_rn(u.y, v.y)));
+  }
+  return make_float2(__fmul_rn(a.x, inv), __fmul_rn(a.y, inv));
+}
+
+__device__ __forceinline__ float2 cross_x2(const float2 *__restrict__ f, long long i,
+                                           long long s1, long long s2, float inv) {
+  float2 total = make_float2(0.0f, 0.0f);
+#pragma unroll
+  for (int g = 0; g < 10; ++g) {
+    const long long a = pair_a(g), b = pair_b(g);
+    const float2 v0 = ldp(f, i + a * s2 + b * s1), v1 = ldp(f, i + a * s2 - b * s1);
+    const float2 v2 = ldp(f, i - a * s2 + b * s1), v3 = ldp(f, i - a * s2 - b * s1);
+    float2 acc;
+    acc.x = __fadd_rn(__fsub_rn(__fsub_rn(v0.x, v1.x), v2.x), v3.x);
+    acc.y = __fadd_rn(__fsub_rn(__fsub_rn(v0.y, v1.y), v2.y), v3.y);
+    if (a != b) {
+      const float2 w0 = ldp(f, i + b * s2 + a * s1), w1 = ldp(f, i + b * s2 - a * s1);
+      const float2 w2 = ldp(f, i - b * s2 + a * s1), w3 = ldp(f, i - b * s2 - a * s1);
+      acc.x = __fadd_rn(__fsub_rn(__fsub_rn(__fadd_rn(acc.x, w0.x), w1.x), w2.x), w3.x);
+      acc.y = __fadd_rn(__fsub_rn(__fsub_rn(__fadd_rn(acc.y, w0.y), w1.y), w2.y), w3.y);
+    }
+    const float w = static_cast<float>(lw(pair_a(g)) * lw(pair_b(g)));
+    const float2 term = make_float2(__fmul_rn(w, acc.x), __fmul_rn(w, acc.y));
+    total = g == 0 ? term
+                   : make_float2(__fadd_rn(total.x, term.x), __fadd_rn(total.y, term.y));
+  }
+  return make_float2(__fmul_rn(total.x, inv), __fmul_rn(total.y, inv));
+}
+
+// h1 / h2 of p (.x) and q (.y) from pair-buffer strides (sX = 1).
+__device__ __forceinline__ void hterms2(const float2 *__restrict__ f, long long i, long long sY,
+                                        long long sZ, const StepParams &prm, float cxx,
+                                        float cyy, float czz, float cxy, float cyz, float cxz,
+                                        H12 *hp, H12 *hq) {
+  const float2 fxx = der2_x2(f, i, 1, prm.dxxinv);
+  const float2 fyy = der2_x2(f, i, sY, prm.dyyinv);
+  const float2 fzz = der2_x2(f, i, sZ, prm.dzzinv);
+  const float2 fxy = cross_x2(f, i, 1, sY, prm.dxyinv);
+  const float2 fyz = cross_x2(f, i, sY, sZ, prm.dyzinv);
+  const float2 fxz = cross_x2(f, i, 1, sZ, prm.dxzinv);
+  const float xx[2] = {fxx.x, fxx.y}, yy[2] = {fyy.x, fyy.y}, zz[2] = {fzz.x, fzz.y};
+  const float xy[2] = {fxy.x, fxy.y}, yz[2] = {fyz.x, fyz.y}, xz[2] = {fxz.x, fxz.y};
+  H12 *out[2] = {hp, hq};
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    float h1 = __fmul_rn(cxx, xx[c]);
+    h1 = __fadd_rn(h1, __fmul_rn(cyy, yy[c]));
+    h1 = __fadd_rn(h1, __fmul_rn(czz, zz[c]));
+    h1 = __fadd_rn(h1, __fmul_rn(cxy, xy[c]));
+    h1 = __fadd_rn(h1, __fmul_rn(cxz, xz[c]));
+    h1 = __fadd_rn(h1, __fmul_rn(cyz, yz[c]));
+    out[c]->h1 = h1;
+    out[c]->h2 = __fsub_rn(__fadd_rn(__fadd_rn(xx[c], yy[c]), zz[c]), h1);
+  }
+}
+
 
 template <int MEDIUM, bool SPONGE>
 __global__ void __launch_bounds__(128)
@@ -152,9 +168,8 @@ __global__ void __launch_bounds__(128)
       v2px = __fmul_rn(v2pz, 1.48f);
       v2pn = __fmul_rn(v2pz, 1.2f);
     }
-    const float *pcf = reinterpret_cast<const float *>(prm.cur);
-    const H12 hp = hterms(pcf, 2 * i, 2, 2 * sY, 2 * sZ, prm, cxx, cyy, czz, cxy, cyz, cxz);
-    const H12 hq = hterms(pcf + 1, 2 * i, 2, 2 * sY, 2 * sZ, prm, cxx, cyy, czz, cxy, cyz, cxz);
+    H12 hp, hq;
+    hterms2(prm.cur, i, sY, sZ, prm, cxx, cyy, czz, cxy, cyz, cxz, &hp, &hq);
     const float h1pmq = __fsub_rn(hp.h1, hq.h1);
     const float h2pmq = __fsub_rn(hp.h2, hq.h2);
     const float rhsp = __fadd_rn(
