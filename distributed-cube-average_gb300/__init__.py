@@ -213,7 +213,11 @@ SIGNATURES = [
                                      C.c_int, C.c_float, C.c_ulonglong, _fp]),
     ("dc_gb300_layer_cells", C.c_longlong, [C.c_long, C.c_long, C.c_long, C.c_int,
                                            C.POINTER(C.c_int), C.c_longlong]),
-    ("dc_gb300_set_learned_layer", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    ("dc_gb300_layer_plan", C.c_int, [C.c_long, C.c_long, C.c_long, C.c_int,
+                                      C.POINTER(C.c_int), C.c_longlong, C.POINTER(C.c_int),
+                                      C.c_longlong, C.POINTER(C.c_longlong),
+                                      C.POINTER(C.c_longlong)]),
+    ("dc_gb300_set_learned_layer",C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     ("dc_gb300_lb_sample", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_long), C.c_int,
                                      C.c_void_p, C.c_void_p, C.c_longlong,
                                      C.POINTER(C.c_longlong)]),
@@ -771,6 +775,22 @@ def layer_cells(sizes, layer: int) -> np.ndarray:
     lib().dc_gb300_layer_cells(*[int(v) for v in sizes], int(layer),
                                out.ctypes.data_as(C.POINTER(C.c_int)), n)
     return out
+
+
+def layer_plan(sizes, layer: int):
+    """(lines, edge): the face lines ([n][4]: x, y, z of the outermost cell,
+    axis | side << 2), corrected in place by one fused pass, and the edge
+    cells ([m][4], ``layer_cells`` entries), corrected through a buffer."""
+    nl, ne = C.c_longlong(), C.c_longlong()
+    dims = [int(v) for v in sizes]
+    check(lib().dc_gb300_layer_plan(*dims, int(layer), None, 0, None, 0, C.byref(nl),
+                                    C.byref(ne)))
+    lines = np.empty((nl.value, 4), np.int32)
+    edge = np.empty((ne.value, 4), np.int32)
+    ip = C.POINTER(C.c_int)
+    check(lib().dc_gb300_layer_plan(*dims, int(layer), lines.ctypes.data_as(ip), nl.value,
+                                    edge.ctypes.data_as(ip), ne.value, C.byref(nl), C.byref(ne)))
+    return lines, edge
 
 
 def set_learned_layer(sim: "Simulation", mlp: "MLP | None", layer: int) -> None:

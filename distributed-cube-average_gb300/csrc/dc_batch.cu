@@ -74,11 +74,20 @@ struct Batch {
   // learned thin layer on every shot (after each step's stencil launches)
   const float *lb_params = nullptr;
   int lb_layer = 0;
-  int4 *d_lb_cells = nullptr;
+  int4 *d_lb_lines = nullptr;  // face lines (meta bits 8..31: the shot)
+  int4 *d_lb_cells = nullptr;  // edge cells
   float2 *d_lb_corr = nullptr;
   LbShot *d_lb_shots = nullptr;
-  long long lb_cells = 0;
+  long long lb_cells = 0;      // corrected cells in all (0: no layer)
+  long long lb_lines = 0, lb_edge = 0;
 };
+
+// Learned-layer launches of one step: the face-line pass, then the edge
+// cells' network and add.
+long lb_launches(const Batch *b) {
+  if (b->lb_cells <= 0) return 0;
+  return (b->lb_lines > 0 ? 1 : 0) + (b->lb_edge > 0 ? 2 : 0);
+}
 
 int fail(int code, const std::string &msg) {
   set_error(msg);
@@ -125,6 +134,7 @@ void release(Batch *b) {
     cudaFree(s.pq[0]);
     cudaFree(s.pq[1]);
   }
+  cudaFree(b->d_lb_lines);
   cudaFree(b->d_lb_cells);
   cudaFree(b->d_lb_corr);
   cudaFree(b->d_lb_shots);
@@ -335,9 +345,10 @@ cudaError_t queue_launches(Batch *b, int cur, int j) {
     if (e != cudaSuccess) return e;
   }
   if (b->lb_cells > 0) {  // learned layer of every shot, after all stencil launches
-    b->launches += 2;
-    return launch_lb_batch_step(b->stream, b->lb_params, b->d_lb_cells, b->lb_cells,
-                                b->d_lb_shots, cur, b->d_lb_corr);
+    b->launches += lb_launches(b);
+    return launch_lb_batch_fused(b->stream, b->lb_params, b->lb_layer, b->d_lb_lines,
+                                 b->lb_lines, b->d_lb_cells, b->lb_edge, b->d_lb_shots, cur,
+                                 b->d_lb_corr);
   }
   return cudaSuccess;
 }
@@ -414,7 +425,7 @@ int run_steps(Batch *b, int steps) {
     }
     BATCH_TRY(cudaGraphLaunch(b->graph[cur], b->stream));
     b->launches += static_cast<long>(kGraphSteps) *
-                       (static_cast<long>(b->groups.size()) + (b->lb_cells > 0 ? 2 : 0)) + 1;
+                       (static_cast<long>(b->groups.size()) + lb_launches(b)) + 1;
     left -= kGraphSteps;
     b->steps_done += kGraphSteps;
   }
@@ -682,40 +693,56 @@ extern "C" int dc_gb300_batch_set_learned_layer(dc_gb300_batch *h, const dc_gb30
   BATCH_TRY(cudaSetDevice(b->device));
   BATCH_TRY(cudaStreamSynchronize(b->stream));
   dcg::drop_graphs(b);
+  cudaFree(b->d_lb_lines);
   cudaFree(b->d_lb_cells);
   cudaFree(b->d_lb_corr);
   cudaFree(b->d_lb_shots);
+  b->d_lb_lines = nullptr;
   b->d_lb_cells = nullptr;
   b->d_lb_corr = nullptr;
   b->d_lb_shots = nullptr;
-  b->lb_cells = 0;
+  b->lb_cells = b->lb_lines = b->lb_edge = 0;
   b->lb_layer = 0;
   b->lb_params = nullptr;
   if (layer == 0) return DC_GB300_OK;
   if (b->shots.size() > (1u << 23)) return fail(DC_GB300_ERR_ARG, "too many shots");
-  std::vector<int4> cells;
+  std::vector<int4> lines, edge;
   std::vector<dcg::LbShot> tab;
+  long long total = 0;
   for (size_t k = 0; k < b->shots.size(); ++k) {
     const dcg::BShot &s = b->shots[k];
     if (s.cfg.sx < 2 * layer + 16 || s.cfg.sy < 2 * layer + 16 || s.cfg.sz < 2 * layer + 16)
       return fail(DC_GB300_ERR_ARG, "every shot's interior must keep at least 8 cells per axis");
-    const std::vector<int4> c = dcg::layer_cells(s.cfg.sx, s.cfg.sy, s.cfg.sz, layer);
-    for (int4 v : c) {
+    const dcg::LayerPlan plan = dcg::layer_plan(s.cfg.sx, s.cfg.sy, s.cfg.sz, layer);
+    for (int4 v : plan.lines) {
       v.w |= static_cast<int>(k) << 8;
-      cells.push_back(v);
+      lines.push_back(v);
     }
+    for (int4 v : plan.edge) {
+      v.w |= static_cast<int>(k) << 8;
+      edge.push_back(v);
+    }
+    total += static_cast<long long>(dcg::layer_cells(s.cfg.sx, s.cfg.sy, s.cfg.sz, layer).size());
     tab.push_back(dcg::LbShot{{s.pq[0], s.pq[1]}, s.pitch, s.plane});
   }
-  const long long n = static_cast<long long>(cells.size());
-  BATCH_TRY(cudaMalloc(&b->d_lb_cells, sizeof(int4) * n));
-  BATCH_TRY(cudaMalloc(&b->d_lb_corr, sizeof(float2) * n));
+  const long long nl = static_cast<long long>(lines.size());
+  const long long ne = static_cast<long long>(edge.size());
+  BATCH_TRY(cudaMalloc(&b->d_lb_lines, sizeof(int4) * std::max(nl, 1LL)));
+  BATCH_TRY(cudaMalloc(&b->d_lb_cells, sizeof(int4) * std::max(ne, 1LL)));
+  BATCH_TRY(cudaMalloc(&b->d_lb_corr, sizeof(float2) * std::max(ne, 1LL)));
   BATCH_TRY(cudaMalloc(&b->d_lb_shots, sizeof(dcg::LbShot) * tab.size()));
-  BATCH_TRY(cudaMemcpyAsync(b->d_lb_cells, cells.data(), sizeof(int4) * n,
-                            cudaMemcpyHostToDevice, b->stream));
+  if (nl > 0)
+    BATCH_TRY(cudaMemcpyAsync(b->d_lb_lines, lines.data(), sizeof(int4) * nl,
+                              cudaMemcpyHostToDevice, b->stream));
+  if (ne > 0)
+    BATCH_TRY(cudaMemcpyAsync(b->d_lb_cells, edge.data(), sizeof(int4) * ne,
+                              cudaMemcpyHostToDevice, b->stream));
   BATCH_TRY(cudaMemcpyAsync(b->d_lb_shots, tab.data(), sizeof(dcg::LbShot) * tab.size(),
                             cudaMemcpyHostToDevice, b->stream));
   BATCH_TRY(cudaStreamSynchronize(b->stream));
-  b->lb_cells = n;
+  b->lb_cells = total;
+  b->lb_lines = nl;
+  b->lb_edge = ne;
   b->lb_layer = layer;
   b->lb_params = dc_gb300_mlp_device_params(mlp);
   return DC_GB300_OK;

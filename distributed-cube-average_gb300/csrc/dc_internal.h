@@ -166,9 +166,12 @@ struct Sim {
   int maps_tx = 0, maps_ty = 0;
   // learned absorbing layer, applied after every stencil pass of a run
   const float *lb_params = nullptr;  // MLP compute parameters (device, owned by the MLP)
-  int4 *d_lb_cells = nullptr;        // layer-cell table
+  int4 *d_lb_cells = nullptr;        // layer-cell table (recorded rollout steps)
   float2 *d_lb_corr = nullptr;       // corrections of one step
   long long lb_cells = 0;
+  int4 *d_lb_lines = nullptr;        // face lines and edge cells (every other step)
+  int4 *d_lb_edge = nullptr;
+  long long lb_lines = 0, lb_edge = 0;
   int lb_layer = 0;
   float *lb_rec = nullptr;           // rollout training: record the step's samples here
   // captured multi-step graphs, keyed by start parity of the pc buffer
@@ -270,6 +273,13 @@ bool encode_tiled(CUtensorMap *map, const void *base, int rank,
 // Learned absorbing layer (dc_learned.cu).  Layer cells of a box with a
 // layer of `layer` cells: {x, y, z, axis | side << 2 | depth << 3}.
 std::vector<int4> layer_cells(long long sx, long long sy, long long sz, int layer);
+// The corrected cells split into face lines (corrected in one fused pass,
+// in place) and edge cells (network into a correction buffer, then added).
+struct LayerPlan {
+  std::vector<int4> lines;  // outermost cell of each face line, meta = axis | side << 2
+  std::vector<int4> edge;   // layer_cells entries
+};
+LayerPlan layer_plan(long long sx, long long sy, long long sz, int layer);
 // Corrections of every layer cell from the new (t+1) and current (t)
 // fields, then added to the new field.
 // `rec` (may be null) also receives every cell's features (sample rows).
@@ -293,6 +303,14 @@ struct LbShot {
 };
 cudaError_t launch_lb_batch_step(cudaStream_t st, const float *params, const int4 *cells,
                                  long long n, const LbShot *shots, int cur_buf, float2 *corr);
+// The in-step correction through the face lines and the edge cells.
+// Bit-identical to launch_lb_step over all corrected cells.
+cudaError_t launch_lb_fused(cudaStream_t st, const float *params, int layer, const int4 *lines,
+                            long long nl, const int4 *edge, long long ne, float2 *nw,
+                            const float2 *cur, long long pitch, long long plane, float2 *corr);
+cudaError_t launch_lb_batch_fused(cudaStream_t st, const float *params, int layer,
+                                  const int4 *lines, long long nl, const int4 *edge, long long ne,
+                                  const LbShot *shots, int cur_buf, float2 *corr);
 // Thin pair buffer <- box of a wide pair buffer at `off`, zero halo.
 cudaError_t launch_crop(cudaStream_t st, float2 *dst, long long sx, long long sy, long long sz,
                         long long pitch, const float2 *src, long long wpitch, long long wplane,

@@ -59,6 +59,7 @@ constexpr int OFF_B3 = OFF_W3 + kOut * kHid;      // [kOut]
 constexpr int kParams = OFF_B3 + kOut;
 static_assert(kParams == DC_GB300_MLP_PARAMS, "parameter count");
 constexpr int kWin = 8;  // cells along the normal
+constexpr int kCorrected = 4;  // outer layer cells corrected by the network
 
 __device__ __forceinline__ bool is_weight(int p) {
   return (p >= OFF_W1 && p < OFF_B1) || (p >= OFF_W2 && p < OFF_B2) || (p >= OFF_W3 && p < OFF_B3);
@@ -460,16 +461,18 @@ struct BatchCellSrc {  // the layer cells of every shot of a batch
 
 // The weights' B fragments live in shared memory (one 8-byte entry per
 // lane and 16 x 8 block, read with one LDS.64 per MMA), which keeps the
-// kernel under 64 registers: eight 4-warp CTAs per SM hide the gathers'
+// kernels under 64 registers: eight 4-warp CTAs per SM hide the gathers'
 // latency.
-template <class Src>
-__global__ void __launch_bounds__(128, 8) lb_tc_kernel(const float *__restrict__ wc, Src src,
-                                                       long long n, float2 *out) {
-  __shared__ float sb1[kDepths * kHid], sb2[kHid], sb3[kOut];
-  __shared__ uint2 bw1[2][4][32], bw2[2][4][32], bw3[2][32];
-  for (int i = threadIdx.x; i < kDepths * kHid; i += blockDim.x) sb1[i] = wc[OFF_B1 + i];
-  if (threadIdx.x < kHid) sb2[threadIdx.x] = wc[OFF_B2 + threadIdx.x];
-  if (threadIdx.x < kOut) sb3[threadIdx.x] = wc[OFF_B3 + threadIdx.x];
+struct NetSmem {
+  float b1[kDepths * kHid], b2[kHid], b3[kOut];
+  uint2 w1[2][4][32], w2[2][4][32], w3[2][32];
+};
+
+// Stages the biases and the weights' B fragments; ends with __syncthreads.
+__device__ __forceinline__ void stage_net(const float *__restrict__ wc, NetSmem &sm) {
+  for (int i = threadIdx.x; i < kDepths * kHid; i += blockDim.x) sm.b1[i] = wc[OFF_B1 + i];
+  if (threadIdx.x < kHid) sm.b2[threadIdx.x] = wc[OFF_B2 + threadIdx.x];
+  if (threadIdx.x < kOut) sm.b3[threadIdx.x] = wc[OFF_B3 + threadIdx.x];
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   if (threadIdx.x < 32) {
     // B fragments: B[k][n] = W[n][k] of each 16 x 8 (k x n) block
@@ -480,18 +483,94 @@ __global__ void __launch_bounds__(128, 8) lb_tc_kernel(const float *__restrict__
       for (int nt = 0; nt < 4; ++nt) {
         const float *r1 = wc + OFF_W1 + (nt * 8 + g) * kIn;
         const float *r2 = wc + OFF_W2 + (nt * 8 + g) * kHid;
-        bw1[kk][nt][lane] = make_uint2(pack_bf16(r1[k0], r1[k0 + 1]),
-                                       pack_bf16(r1[k0 + 8], r1[k0 + 9]));
-        bw2[kk][nt][lane] = make_uint2(pack_bf16(r2[k0], r2[k0 + 1]),
-                                       pack_bf16(r2[k0 + 8], r2[k0 + 9]));
+        sm.w1[kk][nt][lane] = make_uint2(pack_bf16(r1[k0], r1[k0 + 1]),
+                                         pack_bf16(r1[k0 + 8], r1[k0 + 9]));
+        sm.w2[kk][nt][lane] = make_uint2(pack_bf16(r2[k0], r2[k0 + 1]),
+                                         pack_bf16(r2[k0 + 8], r2[k0 + 9]));
       }
       const float *r3 = wc + OFF_W3 + min(g, kOut - 1) * kHid;
-      bw3[kk][lane] = g < kOut ? make_uint2(pack_bf16(r3[k0], r3[k0 + 1]),
-                                            pack_bf16(r3[k0 + 8], r3[k0 + 9]))
-                               : make_uint2(0u, 0u);
+      sm.w3[kk][lane] = g < kOut ? make_uint2(pack_bf16(r3[k0], r3[k0 + 1]),
+                                              pack_bf16(r3[k0 + 8], r3[k0 + 9]))
+                                 : make_uint2(0u, 0u);
     }
   }
   __syncthreads();
+}
+
+// The network over the 16 rows of one warp pass: lane (g, t) brings the
+// features f0 of row g and f1 of row g + 8 (window positions 2t, 2t + 1, in
+// the order of the sample-row loader) and their depths.  Returns false,
+// warp-uniformly, when all 16 rows are silent (no correction anywhere);
+// otherwise the lanes with t == 0 hold the corrections r * y of row g in
+// (rr0 * y[0], rr0 * y[1]) and of row g + 8 in (rr1 * y[2], rr1 * y[3]).
+__device__ __forceinline__ bool net16(const NetSmem &sm, const float f0[8], const float f1[8],
+                                      int d0, int d1, float &rr0, float &rr1, float y[4]) {
+  const int lane = threadIdx.x & 31, t = lane & 3;
+  // rms of each row's 32 features (spread over the 4 lanes of a quad)
+  float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    s0 = fmaf(f0[k], f0[k], s0);
+    s1 = fmaf(f1[k], f1[k], s1);
+  }
+  s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
+  s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+  s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+  s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+  if (__all_sync(0xffffffffu, s0 == 0.f && s1 == 0.f)) return false;
+  rr0 = sqrtf(s0 * (1.0f / kIn));
+  rr1 = sqrtf(s1 * (1.0f / kIn));
+  const float i0 = rr0 > 0.f ? 1.0f / rr0 : 0.f, i1 = rr1 > 0.f ? 1.0f / rr1 : 0.f;
+  uint32_t a[2][4];
+#pragma unroll
+  for (int kk = 0; kk < 2; ++kk) {
+    a[kk][0] = pack_bf16(f0[4 * kk] * i0, f0[4 * kk + 1] * i0);
+    a[kk][1] = pack_bf16(f1[4 * kk] * i1, f1[4 * kk + 1] * i1);
+    a[kk][2] = pack_bf16(f0[4 * kk + 2] * i0, f0[4 * kk + 3] * i0);
+    a[kk][3] = pack_bf16(f1[4 * kk + 2] * i1, f1[4 * kk + 3] * i1);
+  }
+  float acc[4][4];
+  // layer 1 (bias per depth)
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt) {
+    const int c = nt * 8 + 2 * t;
+    acc[nt][0] = sm.b1[d0 * kHid + c];
+    acc[nt][1] = sm.b1[d0 * kHid + c + 1];
+    acc[nt][2] = sm.b1[d1 * kHid + c];
+    acc[nt][3] = sm.b1[d1 * kHid + c + 1];
+    const uint2 b0 = sm.w1[0][nt][lane], b1 = sm.w1[1][nt][lane];
+    mma_bf16(acc[nt], a[0], b0.x, b0.y);
+    mma_bf16(acc[nt], a[1], b1.x, b1.y);
+  }
+  gelu_to_a(acc, a);
+  // layer 2
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt) {
+    const int c = nt * 8 + 2 * t;
+    acc[nt][0] = acc[nt][2] = sm.b2[c];
+    acc[nt][1] = acc[nt][3] = sm.b2[c + 1];
+    const uint2 b0 = sm.w2[0][nt][lane], b1 = sm.w2[1][nt][lane];
+    mma_bf16(acc[nt], a[0], b0.x, b0.y);
+    mma_bf16(acc[nt], a[1], b1.x, b1.y);
+  }
+  gelu_to_a(acc, a);
+  // layer 3: outputs in columns 0 and 1, held by the lanes with t == 0
+  y[0] = y[2] = t == 0 ? sm.b3[0] : 0.f;
+  y[1] = y[3] = t == 0 ? sm.b3[1] : 0.f;
+  const uint2 b0 = sm.w3[0][lane], b1 = sm.w3[1][lane];
+  mma_bf16(y, a[0], b0.x, b0.y);
+  mma_bf16(y, a[1], b1.x, b1.y);
+  return true;
+}
+
+// One correction per cell or sample row, written to out (zeros for silent
+// rows): the training-side and recorded-rollout evaluation.
+template <class Src>
+__global__ void __launch_bounds__(128, 8) lb_tc_kernel(const float *__restrict__ wc, Src src,
+                                                       long long n, float2 *out) {
+  __shared__ NetSmem sm;
+  stage_net(wc, sm);
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
   for (long long base = warp * 16; base < n; base += nwarps * 16) {
@@ -510,72 +589,140 @@ __global__ void __launch_bounds__(128, 8) lb_tc_kernel(const float *__restrict__
 #pragma unroll
       for (int k = 0; k < 8; ++k) f1[k] = 0.f;
     }
-    // rms of each cell's 32 features (spread over the 4 lanes of a quad)
-    float s0 = 0.f, s1 = 0.f;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      s0 = fmaf(f0[k], f0[k], s0);
-      s1 = fmaf(f1[k], f1[k], s1);
-    }
-    s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
-    s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
-    s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
-    s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
-    if (__all_sync(0xffffffffu, s0 == 0.f && s1 == 0.f)) {  // 16 silent cells: no correction
-      if (t == 0) {
-        if (r0 < n) out[r0] = make_float2(0.f, 0.f);
-        if (r1 < n) out[r1] = make_float2(0.f, 0.f);
-      }
-      continue;
-    }
-    const float rr0 = sqrtf(s0 * (1.0f / kIn)), rr1 = sqrtf(s1 * (1.0f / kIn));
-    const float i0 = rr0 > 0.f ? 1.0f / rr0 : 0.f, i1 = rr1 > 0.f ? 1.0f / rr1 : 0.f;
-    uint32_t a[2][4];
-#pragma unroll
-    for (int kk = 0; kk < 2; ++kk) {
-      a[kk][0] = pack_bf16(f0[4 * kk] * i0, f0[4 * kk + 1] * i0);
-      a[kk][1] = pack_bf16(f1[4 * kk] * i1, f1[4 * kk + 1] * i1);
-      a[kk][2] = pack_bf16(f0[4 * kk + 2] * i0, f0[4 * kk + 3] * i0);
-      a[kk][3] = pack_bf16(f1[4 * kk + 2] * i1, f1[4 * kk + 3] * i1);
-    }
-    float acc[4][4];
-    // layer 1 (bias per depth)
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-      const int c = nt * 8 + 2 * t;
-      acc[nt][0] = sb1[d0 * kHid + c];
-      acc[nt][1] = sb1[d0 * kHid + c + 1];
-      acc[nt][2] = sb1[d1 * kHid + c];
-      acc[nt][3] = sb1[d1 * kHid + c + 1];
-      const uint2 b0 = bw1[0][nt][lane], b1 = bw1[1][nt][lane];
-      mma_bf16(acc[nt], a[0], b0.x, b0.y);
-      mma_bf16(acc[nt], a[1], b1.x, b1.y);
-    }
-    gelu_to_a(acc, a);
-    // layer 2
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-      const int c = nt * 8 + 2 * t;
-      acc[nt][0] = acc[nt][2] = sb2[c];
-      acc[nt][1] = acc[nt][3] = sb2[c + 1];
-      const uint2 b0 = bw2[0][nt][lane], b1 = bw2[1][nt][lane];
-      mma_bf16(acc[nt], a[0], b0.x, b0.y);
-      mma_bf16(acc[nt], a[1], b1.x, b1.y);
-    }
-    gelu_to_a(acc, a);
-    // layer 3: outputs in columns 0 and 1, held by the lanes with t == 0
-    float y[4];
-    y[0] = y[2] = t == 0 ? sb3[0] : 0.f;
-    y[1] = y[3] = t == 0 ? sb3[1] : 0.f;
-    {
-      const uint2 b0 = bw3[0][lane], b1 = bw3[1][lane];
-      mma_bf16(y, a[0], b0.x, b0.y);
-      mma_bf16(y, a[1], b1.x, b1.y);
-    }
+    float rr0 = 0.f, rr1 = 0.f, y[4];
+    const bool live = net16(sm, f0, f1, d0, d1, rr0, rr1, y);
     if (t == 0) {
-      if (r0 < n) out[r0] = make_float2(rr0 * y[0], rr0 * y[1]);
-      if (r1 < n) out[r1] = make_float2(rr1 * y[2], rr1 * y[3]);
+      if (r0 < n) out[r0] = live ? make_float2(rr0 * y[0], rr0 * y[1]) : make_float2(0.f, 0.f);
+      if (r1 < n) out[r1] = live ? make_float2(rr1 * y[2], rr1 * y[3]) : make_float2(0.f, 0.f);
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fused in-step correction of the face lines.  A face line is the kLine
+// corrected cells of one boundary normal (outermost first) whose tangential
+// coordinates lie far enough inside the other two axes' interiors that no
+// other line's cell is in its windows and no other cell's window reaches it
+// (layer_plan below); its kLine windows span kLineCells distinct cells.  One
+// warp takes 4 lines -- the 16 rows of one MMA pass: it gathers the 4 x
+// kLineCells cells of both time levels once into shared memory, evaluates
+// the network and adds each correction in place.  Every value a warp reads
+// was read before it writes, and no other warp touches its lines, so the
+// result is bit-identical to the two-pass form (lb_tc_kernel then
+// lb_add_kernel) while reading each cell once instead of up to 8 times.
+constexpr int kLine = kCorrected;               // corrected cells per line
+constexpr int kLineCells = kLine + kWin - 1;    // cells the line's windows span
+constexpr int kLineWarp = 16 / kLine;           // lines per warp pass
+constexpr int kGather = 2 * kLineCells * kLineWarp;  // float2 loads per warp pass
+constexpr int kGatherPerLane = (kGather + 31) / 32;
+static_assert(16 % kLine == 0 && 32 % kLineWarp == 0, "line packing of the MMA rows");
+
+struct LinePtr {
+  float2 *nw;         // the line's outermost cell in the new field
+  const float2 *cur;  // ... in the current field
+  long long step;     // inward stride
+};
+
+__device__ __forceinline__ long long inward_step(int code, long long pitch, long long plane) {
+  const int axis = code & 3, side = (code >> 2) & 1;
+  const long long stride = axis == 0 ? 1 : axis == 1 ? pitch : plane;
+  return side ? -stride : stride;
+}
+
+struct LineSrc {  // the face lines of one simulation
+  const int4 *lines;
+  float2 *nw;
+  const float2 *cur;
+  long long pitch, plane;
+  __device__ __forceinline__ LinePtr get(long long l) const {
+    const int4 c = lines[l];
+    const long long g = static_cast<long long>(c.z) * plane + static_cast<long long>(c.y) * pitch + c.x;
+    return LinePtr{nw + g, cur + g, inward_step(c.w, pitch, plane)};
+  }
+};
+
+struct BatchLineSrc {  // the face lines of every shot of a batch
+  const int4 *lines;
+  const LbShot *shots;
+  int cur_buf;
+  __device__ __forceinline__ LinePtr get(long long l) const {
+    const int4 c = lines[l];
+    const LbShot &sh = shots[c.w >> 8];
+    const long long g = static_cast<long long>(c.z) * sh.plane +
+                        static_cast<long long>(c.y) * sh.pitch + c.x;
+    return LinePtr{sh.pq[1 - cur_buf] + g, sh.pq[cur_buf] + g,
+                   inward_step(c.w, sh.pitch, sh.plane)};
+  }
+};
+
+template <class Src>
+__global__ void __launch_bounds__(128, 8) lb_line_kernel(const float *__restrict__ wc, Src src,
+                                                         long long nlines, int layer) {
+  __shared__ NetSmem sm;
+  // per warp: [field][cell][line] (field 0 = new, 1 = current), and the
+  // lines' new-field pointers and strides for the writes
+  __shared__ float2 sl[4][2][kLineCells][kLineWarp];
+  __shared__ float2 *snw[4][kLineWarp];
+  __shared__ long long sst[4][kLineWarp];
+  stage_net(wc, sm);
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
+  const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+  // rows g and g + 8: position j of lines la and lb
+  const int j = g % kLine, la = g / kLine, lb = la + 8 / kLine;
+  const int depth = layer - 1 - j;
+  for (long long base = warp * kLineWarp; base < nlines; base += nwarps * kLineWarp) {
+    // lane serves line lane % 4 in the gather (32 is a multiple of 4)
+    const int ml = lane % kLineWarp;
+    const bool mv = base + ml < nlines;
+    LinePtr lp{nullptr, nullptr, 0};
+    if (mv) lp = src.get(base + ml);
+    if (lane < kLineWarp) {
+      snw[w][lane] = lp.nw;
+      sst[w][lane] = lp.step;
+    }
+    float2 v[kGatherPerLane];
+#pragma unroll
+    for (int k = 0; k < kGatherPerLane; ++k) {  // all loads first, then the stores
+      const int i = lane + 32 * k;
+      const int fld = i / (kLineCells * kLineWarp), c = (i / kLineWarp) % kLineCells;
+      v[k] = make_float2(0.f, 0.f);
+      if (mv && i < kGather) v[k] = fld ? lp.cur[c * lp.step] : lp.nw[c * lp.step];
+    }
+#pragma unroll
+    for (int k = 0; k < kGatherPerLane; ++k) {
+      const int i = lane + 32 * k;
+      const int fld = i / (kLineCells * kLineWarp), c = (i / kLineWarp) % kLineCells;
+      if (i < kGather) sl[w][fld][c][ml] = v[k];
+    }
+    __syncwarp();
+    float f0[8], f1[8];
+    {
+      const int c0 = j + 2 * t, c1 = c0 + 1;
+      const float2 a0 = sl[w][0][c0][la], a1 = sl[w][0][c1][la];
+      const float2 b0 = sl[w][1][c0][la], b1 = sl[w][1][c1][la];
+      f0[0] = a0.x, f0[1] = a1.x, f0[2] = a0.y, f0[3] = a1.y;
+      f0[4] = b0.x, f0[5] = b1.x, f0[6] = b0.y, f0[7] = b1.y;
+      const float2 e0 = sl[w][0][c0][lb], e1 = sl[w][0][c1][lb];
+      const float2 h0 = sl[w][1][c0][lb], h1 = sl[w][1][c1][lb];
+      f1[0] = e0.x, f1[1] = e1.x, f1[2] = e0.y, f1[3] = e1.y;
+      f1[4] = h0.x, f1[5] = h1.x, f1[6] = h0.y, f1[7] = h1.y;
+    }
+    float rr0 = 0.f, rr1 = 0.f, y[4];
+    if (net16(sm, f0, f1, depth, depth, rr0, rr1, y) && t == 0) {
+      // new value = stencil output + correction, rounded as the two-pass form
+      if (base + la < nlines) {
+        const float2 v = sl[w][0][j][la];
+        snw[w][la][j * sst[w][la]] = make_float2(__fadd_rn(v.x, __fmul_rn(rr0, y[0])),
+                                                 __fadd_rn(v.y, __fmul_rn(rr0, y[1])));
+      }
+      if (base + lb < nlines) {
+        const float2 v = sl[w][0][j][lb];
+        snw[w][lb][j * sst[w][lb]] = make_float2(__fadd_rn(v.x, __fmul_rn(rr1, y[2])),
+                                                 __fadd_rn(v.y, __fmul_rn(rr1, y[3])));
+      }
+    }
+    __syncwarp();  // the next pass overwrites this warp's staging
   }
 }
 
@@ -668,8 +815,6 @@ int grid_for(long long n, int per_block) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-constexpr int kCorrected = 4;  // outer layer cells corrected by the network
-
 std::vector<int4> layer_cells(long long sx, long long sy, long long sz, int layer) {
   std::vector<int4> out;
   const long long s[3] = {sx, sy, sz};
@@ -727,6 +872,67 @@ cudaError_t launch_lb_batch_step(cudaStream_t st, const float *wc, const int4 *c
   if (e != cudaSuccess) return e;
   lb_add_batch_kernel<<<grid_for(n, 256), 256, 0, st>>>(cells, n, shots, cur_buf, corr);
   return cudaGetLastError();
+}
+
+// Splits the corrected cells into face lines (entries for the outermost
+// cell, meta = axis | side << 2) and the remaining edge cells (layer_cells
+// entries).  The windows of the least deep corrected cells reach m cells
+// past the layer into the interior; a line is a face line when both of its
+// tangential coordinates lie at least m + 1 cells inside the other axes'
+// interiors.  Then (a) every cell a face line reads has those tangential
+// coordinates, so it is the line's own or an interior cell, and (b) no edge
+// cell's window reaches a face line's cell: a window along the line's axis
+// keeps the edge cell's tangential coordinates, and one along another axis
+// stays within m cells of that axis' layer.  So the face lines and the edge
+// cells can be corrected independently.
+LayerPlan layer_plan(long long sx, long long sy, long long sz, int layer) {
+  LayerPlan plan;
+  const std::vector<int4> cells = layer_cells(sx, sy, sz, layer);
+  if (layer < kCorrected) {
+    plan.edge = cells;
+    return plan;
+  }
+  const int m = std::max(0, kWin - 1 - (layer - kCorrected));
+  const long long s[3] = {sx, sy, sz};
+  auto inside = [&](int a, long long c) {
+    return c >= 4 + layer + m && c < s[a] - 4 - layer - m;
+  };
+  for (const int4 &c : cells) {
+    const int axis = c.w & 3, depth = (c.w >> 3) & 31;
+    const long long p[3] = {c.x, c.y, c.z};
+    const int a1 = (axis + 1) % 3, a2 = (axis + 2) % 3;
+    if (!(inside(a1, p[a1]) && inside(a2, p[a2])))
+      plan.edge.push_back(c);
+    else if (depth == layer - 1)
+      plan.lines.push_back(make_int4(c.x, c.y, c.z, c.w & 7));
+  }
+  return plan;
+}
+
+cudaError_t launch_lb_fused(cudaStream_t st, const float *wc, int layer, const int4 *lines,
+                            long long nl, const int4 *edge, long long ne, float2 *nw,
+                            const float2 *cur, long long pitch, long long plane, float2 *corr) {
+  if (nl > 0) {
+    lb_line_kernel<LineSrc><<<grid_for(nl, 4 * kLineWarp), 128, 0, st>>>(
+        wc, LineSrc{lines, nw, cur, pitch, plane}, nl, layer);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (ne > 0) return launch_lb_step(st, wc, edge, ne, nw, cur, pitch, plane, corr, nullptr);
+  return cudaSuccess;
+}
+
+cudaError_t launch_lb_batch_fused(cudaStream_t st, const float *wc, int layer, const int4 *lines,
+                                  long long nl, const int4 *edge, long long ne,
+                                  const LbShot *shots, int cur_buf, float2 *corr) {
+  if (nl > 0) {
+    lb_line_kernel<BatchLineSrc><<<grid_for(nl, 4 * kLineWarp), 128, 0, st>>>(
+        wc, BatchLineSrc{lines, shots, cur_buf}, nl, layer);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (ne > 0) return launch_lb_batch_step(st, wc, edge, ne, shots, cur_buf, corr);
+  return cudaSuccess;
 }
 
 cudaError_t launch_lb_sample(cudaStream_t st, const int4 *cells, long long n, const float2 *nw,
@@ -966,6 +1172,30 @@ extern "C" long long dc_gb300_layer_cells(long sx, long sy, long sz, int layer, 
       cells[4 * i + 3] = v[i].w;
     }
   return n;
+}
+
+extern "C" int dc_gb300_layer_plan(long sx, long sy, long sz, int layer, int *lines,
+                                   long long lines_cap, int *edge, long long edge_cap,
+                                   long long *n_lines, long long *n_edge) {
+  if (!n_lines || !n_edge) return fail(DC_GB300_ERR_ARG, "null count");
+  if (layer < 1 || layer > DC_GB300_MLP_DEPTHS || sx < 2 * layer + 16 || sy < 2 * layer + 16 ||
+      sz < 2 * layer + 16)
+    return fail(DC_GB300_ERR_ARG, "invalid layer geometry");
+  const dcg::LayerPlan p = dcg::layer_plan(sx, sy, sz, layer);
+  auto put = [](const std::vector<int4> &v, int *out, long long cap) {
+    if (!out) return;
+    for (long long i = 0; i < std::min(static_cast<long long>(v.size()), cap); ++i) {
+      out[4 * i] = v[i].x;
+      out[4 * i + 1] = v[i].y;
+      out[4 * i + 2] = v[i].z;
+      out[4 * i + 3] = v[i].w;
+    }
+  };
+  put(p.lines, lines, lines_cap);
+  put(p.edge, edge, edge_cap);
+  *n_lines = static_cast<long long>(p.lines.size());
+  *n_edge = static_cast<long long>(p.edge.size());
+  return DC_GB300_OK;
 }
 
 extern "C" const float *dc_gb300_mlp_device_params(const dc_gb300_mlp *m) {

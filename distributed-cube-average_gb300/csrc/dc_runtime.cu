@@ -105,6 +105,18 @@ void drop_graphs(Sim *s) {
   }
 }
 
+void free_layer(Sim *s) {
+  cudaFree(s->d_lb_cells);
+  cudaFree(s->d_lb_corr);
+  cudaFree(s->d_lb_lines);
+  cudaFree(s->d_lb_edge);
+  s->d_lb_cells = s->d_lb_lines = s->d_lb_edge = nullptr;
+  s->d_lb_corr = nullptr;
+  s->lb_cells = s->lb_lines = s->lb_edge = 0;
+  s->lb_layer = 0;
+  s->lb_params = nullptr;
+}
+
 void release(Sim *s) {
   if (!s) return;
   if (s->stream) cudaStreamSynchronize(s->stream);
@@ -126,8 +138,7 @@ void release(Sim *s) {
   cudaFree(s->d_energy);
   cudaFree(s->d_step);
   cudaFree(s->d_err);
-  cudaFree(s->d_lb_cells);
-  cudaFree(s->d_lb_corr);
+  free_layer(s);
   if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -210,6 +221,13 @@ void swap_roles(dc_device_data *a) {
   std::swap(a->qp, a->qc);
 }
 
+// Kernel launches of one step: the stencil pass, then with a learned layer
+// the face-line pass and the edge cells' network and add.
+long long launches_per_step(const Sim *s) {
+  if (s->lb_cells <= 0) return 1;
+  return 1 + (s->lb_lines > 0 ? 1 : 0) + (s->lb_edge > 0 ? 2 : 0);
+}
+
 // Queues one full time step (j-th of a run): fused source for the next
 // step, stencil over [4, s-4)^3, receiver gather; then swaps the roles.
 cudaError_t queue_step(Sim *s, int j) {
@@ -245,9 +263,16 @@ cudaError_t queue_step(Sim *s, int j) {
   if (s->lb_cells > 0) {  // learned layer: correct the new field's layer cells
     int cur = -1, prev = -1;
     roles(s, &cur, &prev);
-    s->launches += 2;
-    e = launch_lb_step(s->stream, s->lb_params, s->d_lb_cells, s->lb_cells, s->pq[prev],
-                       s->pq[cur], s->pitch, s->plane, s->d_lb_corr, s->lb_rec);
+    if (s->lb_rec) {  // recorded rollout step: every cell's features in table order
+      s->launches += 2;
+      e = launch_lb_step(s->stream, s->lb_params, s->d_lb_cells, s->lb_cells, s->pq[prev],
+                         s->pq[cur], s->pitch, s->plane, s->d_lb_corr, s->lb_rec);
+    } else {
+      s->launches += launches_per_step(s) - 1;
+      e = launch_lb_fused(s->stream, s->lb_params, s->lb_layer, s->d_lb_lines, s->lb_lines,
+                          s->d_lb_edge, s->lb_edge, s->pq[prev], s->pq[cur], s->pitch,
+                          s->plane, s->d_lb_corr);
+    }
     if (e != cudaSuccess) return e;
   }
   swap_roles(&s->handle->abi);
@@ -915,22 +940,29 @@ extern "C" int dc_gb300_set_learned_layer(dc_gb300_sim *h, const dc_gb300_mlp *m
   DCG_TRY(cudaStreamSynchronize(s->stream));
   drop_graphs(s);
   ++s->config_version;
-  cudaFree(s->d_lb_cells);
-  cudaFree(s->d_lb_corr);
-  s->d_lb_cells = nullptr;
-  s->d_lb_corr = nullptr;
-  s->lb_cells = 0;
-  s->lb_layer = 0;
-  s->lb_params = nullptr;
+  free_layer(s);
   if (layer == 0) return DC_GB300_OK;
   const std::vector<int4> cells = layer_cells(s->sx, s->sy, s->sz, layer);
+  const LayerPlan plan = layer_plan(s->sx, s->sy, s->sz, layer);
   const long long n = static_cast<long long>(cells.size());
+  const long long nl = static_cast<long long>(plan.lines.size());
+  const long long ne = static_cast<long long>(plan.edge.size());
   DCG_TRY(cudaMalloc(&s->d_lb_cells, sizeof(int4) * n));
   DCG_TRY(cudaMalloc(&s->d_lb_corr, sizeof(float2) * n));
+  DCG_TRY(cudaMalloc(&s->d_lb_lines, sizeof(int4) * std::max(nl, 1LL)));
+  DCG_TRY(cudaMalloc(&s->d_lb_edge, sizeof(int4) * std::max(ne, 1LL)));
   DCG_TRY(cudaMemcpyAsync(s->d_lb_cells, cells.data(), sizeof(int4) * n, cudaMemcpyHostToDevice,
                           s->stream));
+  if (nl > 0)
+    DCG_TRY(cudaMemcpyAsync(s->d_lb_lines, plan.lines.data(), sizeof(int4) * nl,
+                            cudaMemcpyHostToDevice, s->stream));
+  if (ne > 0)
+    DCG_TRY(cudaMemcpyAsync(s->d_lb_edge, plan.edge.data(), sizeof(int4) * ne,
+                            cudaMemcpyHostToDevice, s->stream));
   DCG_TRY(cudaStreamSynchronize(s->stream));
   s->lb_cells = n;
+  s->lb_lines = nl;
+  s->lb_edge = ne;
   s->lb_layer = layer;
   s->lb_params = dc_gb300_mlp_device_params(mlp);
   return DC_GB300_OK;
@@ -1166,8 +1198,6 @@ int capture_chunk(Sim *s, cudaGraphExec_t *out) {
     return fail(DC_GB300_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   return DC_GB300_OK;
 }
-
-long long launches_per_step(const Sim *s) { return s->lb_cells > 0 ? 3 : 1; }
 
 }  // namespace
 

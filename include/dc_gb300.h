@@ -480,6 +480,15 @@ int dc_gb300_mlp_train(dc_gb300_mlp *mlp, const float *samples, const float *tar
  * depth 0 = next to the interior).  Writes at most `cap` entries (cells may
  * be NULL) and returns the count, or -1 on invalid geometry.  Host only. */
 long long dc_gb300_layer_cells(long sx, long sy, long sz, int layer, int *cells, long long cap);
+/* How a step applies the layer: the corrected cells split into face lines,
+ * corrected in place by one fused pass, and edge cells, whose corrections
+ * are computed into a buffer and then added.  lines[4*i..4*i+3] = x, y, z of
+ * a line's outermost cell and axis | side << 2 (the line is the 4 cells
+ * from there inward); edge[] holds dc_gb300_layer_cells entries.  Writes at
+ * most lines_cap / edge_cap entries (either array may be NULL) and the
+ * counts to *n_lines / *n_edge; returns DC_GB300_OK or an error.  Host only. */
+int dc_gb300_layer_plan(long sx, long sy, long sz, int layer, int *lines, long long lines_cap,
+                        int *edge, long long edge_cap, long long *n_lines, long long *n_edge);
 /* Applies the MLP after every stencil pass of dc_gb300_run to the layer
  * cells of a layer `layer` cells wide (1..DC_GB300_MLP_DEPTHS; 0 turns it
  * off).  The simulation reads the MLP's parameters at every step: keep the

@@ -7,6 +7,8 @@
 * Training on the GPU fits a teacher network's outputs (loss down 20x).
 * In a simulation step, the layer cells receive exactly r * MLP(features)
   of the stencil's output, every other cell is untouched.
+* The fused step (face lines in place, edge cells through a buffer) is
+  bit-identical to the per-cell two-pass form of recorded rollout steps.
 * What the trained network gains: on a 48^3 interior with an 8-cell layer,
   reflected energy in a 12-cell band next to the interior's boundary, for
   shots not seen in training, against the same thin layer without it.
@@ -116,6 +118,54 @@ def test_learned_layer_step_applies_corrections(dc, torch):
     mask = np.ones(shape, bool)
     mask[cells[:, 2], cells[:, 1], cells[:, 0]] = False
     assert not np.any(dp[mask]) and not np.any(dq[mask])
+
+
+def test_fused_layer_step_matches_recorded_step(dc, torch):
+    """A step corrects the face lines in place in one fused pass and the
+    edge cells through a buffer; a recorded rollout step runs the per-cell
+    two-pass form over every corrected cell.  From the same cropped state,
+    both give bit-identical fields."""
+    from dc_gb300 import learned
+    layer, steps = 8, 6
+    wide_sizes, thin_sizes, off = (64, 62, 60), (44, 42, 40), (9, 10, 11)
+    rng = np.random.default_rng(5)
+    values = (0.15, 0.35, 0.5, 0.45, 0.84, 0.54, 4.0e6, 3.0e6, 1.0e6, 3.5e6)
+    wshape, tshape = wide_sizes[::-1], thin_sizes[::-1]
+    fields = [rng.normal(0, 1, wshape).astype(np.float32) for _ in range(4)]
+    for f in fields:
+        f[:4], f[-4:], f[:, :4], f[:, -4:], f[:, :, :4], f[:, :, -4:] = 0, 0, 0, 0, 0, 0
+    (ox, oy, oz), (tx, ty, tz) = off, thin_sizes
+    crop = []
+    for f in fields:  # the thin box's view of the wide fields, zero halo
+        c = np.zeros(tshape, np.float32)
+        c[4:-4, 4:-4, 4:-4] = f[oz + 4:oz + tz - 4, oy + 4:oy + ty - 4, ox + 4:ox + tx - 4]
+        crop.append(c)
+    lines, edge = dc.layer_plan(thin_sizes, layer)
+    assert len(lines) > 0 and len(edge) > 0
+    n = len(dc.layer_cells(thin_sizes, layer))
+    xs = torch.empty(n * steps * 33, dtype=torch.float32, device="cuda")
+    ts = torch.empty(n * steps * 2, dtype=torch.float32, device="cuda")
+    sim = lambda s: dc.Simulation(s, (12.5,) * 3, 0.5e-3, kernel=dc.KERNEL_FAST,  # noqa: E731
+                                  device=0)
+    with dc.MLP(device=0, params=np.load(learned.WEIGHTS)) as m, sim(wide_sizes) as wide, \
+            sim(thin_sizes) as rec, sim(thin_sizes) as fused:
+        wide.set_precomp([np.full(wshape, v, np.float32) for v in values])
+        wide.set_fields(*fields)
+        for t in (rec, fused):
+            t.set_precomp([np.full(tshape, v, np.float32) for v in values])
+            dc.set_learned_layer(t, m, layer)
+        rec.set_fields()
+        fused.set_fields(*crop)
+        assert dc.lb_rollout(wide, rec, off, steps, xs.data_ptr(), ts.data_ptr(),
+                             n * steps) == n * steps
+        rec.synchronize()
+        fused.run(steps)
+        fused.synchronize()
+        a, b = rec.get_fields(), fused.get_fields()
+    for k in ("pp", "pc", "qp", "qc"):
+        assert np.array_equal(a[k], b[k]), k
+    # the network did act: the recorded rows carry live features
+    assert float(xs.abs().max()) > 0
 
 
 def test_trained_layer_reduces_reflections(dc, torch):

@@ -61,3 +61,46 @@ def test_layer_cell_table_matches_direct_enumeration(dc):
     for x, y, z, m in got:
         assert want[(x, y, z)] == (m & 3, m >> 3, (m >> 2) & 1)
     assert want[(4, 4, 10)] == (0, layer - 1, 0)  # tie: lowest axis
+
+
+def _inward(cell, axis, side, k):
+    c = list(cell)
+    c[axis] += k if side == 0 else -k
+    return tuple(c)
+
+
+@pytest.mark.parametrize("s,layer", [((40, 38, 36), 6), ((44, 46, 45), 8), ((32, 33, 32), 8),
+                                     ((30, 30, 31), 4), ((28, 29, 30), 3)])
+def test_layer_plan_partitions_and_separates(dc, s, layer):
+    """The step's split of the corrected cells: face lines (4 cells from the
+    outermost inward, corrected in place from windows spanning 11 cells)
+    and edge cells (8-cell windows, corrected through a buffer) cover every
+    corrected cell once, and no line's or edge cell's window reads a cell
+    that another line or the edge pass writes -- so the fused step equals
+    the two-pass one."""
+    cells = {(x, y, z): m for x, y, z, m in dc.layer_cells(s, layer)}
+    lines, edge = dc.layer_plan(s, layer)
+    if layer < 4:
+        assert len(lines) == 0
+    elif min(s) >= 2 * layer + 16 + 2 * (11 - layer):
+        assert len(lines) > 0
+    owner, line_reads = {}, []
+    for i, (x, y, z, m) in enumerate(lines):
+        axis, side = m & 3, (m >> 2) & 1
+        for j in range(4):
+            c = _inward((x, y, z), axis, side, j)
+            assert cells[c] == axis | side << 2 | (layer - 1 - j) << 3
+            assert c not in owner
+            owner[c] = i
+        line_reads.append([_inward((x, y, z), axis, side, k) for k in range(11)])
+    edge_cells = {(x, y, z) for x, y, z, _ in edge}
+    assert len(edge_cells) == len(edge)
+    assert not edge_cells & owner.keys()
+    assert edge_cells | owner.keys() == cells.keys()
+    for i, reads in enumerate(line_reads):
+        for c in reads:
+            assert owner.get(c, i) == i and c not in edge_cells
+    for x, y, z, m in edge:
+        axis, side = m & 3, (m >> 2) & 1
+        for k in range(8):
+            assert _inward((x, y, z), axis, side, k) not in owner
