@@ -253,6 +253,7 @@ int prepare(Batch *b, int ty, int zsplit, bool persistent) {
   fill_weights(&common, b->dx, b->dy, b->dz, b->dt);
   if (b->coef_form == CF_F16 || b->coef_form == CF_BF16)
     common.dt2 = ldexpf(common.dt2, b->vexp);
+    common.dt2_iso = ldexpf(common.dt2_iso, b->vexp);
   b->groups.clear();
   long long max_items = 0;
   for (int g0 = 0; g0 < n; g0 += kMaxBatchShots) {

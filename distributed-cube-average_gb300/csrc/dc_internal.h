@@ -69,6 +69,7 @@ struct StepParams {
   float w2x[5], w2y[5], w2z[5];  // K_i / da^2 (second derivative)
   float w1x[4], w1y[4], w1z[4];  // L_i / da   (first derivative, i = 1..4)
   float dt, dt2;
+  float dt2_iso;  // dt2 / d^2 when dx = dy = dz (unscaled weights in the stencil)
   // Wavefields are stored as interleaved (p, q) pairs: `prev` holds
   // (pp, qp) and is updated in place, `cur` holds (pc, qc).
   float2 *prev;

@@ -655,56 +655,79 @@ struct BatchLineSrc {  // the face lines of every shot of a batch
   }
 };
 
+// Asynchronous 8-byte copy global -> shared (zero fill when !valid; gsrc
+// must still be a mapped address).
+__device__ __forceinline__ void cp_async8(void *sdst, const void *gsrc, bool valid) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(sdst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(gsrc),
+               "r"(valid ? 8 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait1() {
+  asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+}
+
+// Each warp double-buffers its staging: the copies of the next pass are in
+// flight (cp.async, no registers held) while the network runs on this one.
 template <class Src>
 __global__ void __launch_bounds__(128, 8) lb_line_kernel(const float *__restrict__ wc, Src src,
                                                          long long nlines, int layer) {
   __shared__ NetSmem sm;
-  // per warp: [field][cell][line] (field 0 = new, 1 = current), and the
-  // lines' new-field pointers and strides for the writes
-  __shared__ float2 sl[4][2][kLineCells][kLineWarp];
-  __shared__ float2 *snw[4][kLineWarp];
-  __shared__ long long sst[4][kLineWarp];
+  // per warp and buffer: [field][cell][line] (field 0 = new, 1 = current),
+  // and the lines' new-field pointers and strides for the writes
+  __shared__ __align__(16) float2 sl[4][2][2][kLineCells][kLineWarp];
+  __shared__ float2 *snw[4][2][kLineWarp];
+  __shared__ long long sst[4][2][kLineWarp];
   stage_net(wc, sm);
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
   const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+  const long long stride = nwarps * kLineWarp;
   // rows g and g + 8: position j of lines la and lb
   const int j = g % kLine, la = g / kLine, lb = la + 8 / kLine;
   const int depth = layer - 1 - j;
-  for (long long base = warp * kLineWarp; base < nlines; base += nwarps * kLineWarp) {
-    // lane serves line lane % 4 in the gather (32 is a multiple of 4)
-    const int ml = lane % kLineWarp;
+  const int ml = lane % kLineWarp;  // the line this lane copies (32 is a multiple of 4)
+  // queues the copies of the pass at `base` into buffer `buf`
+  auto gather = [&](long long base, int buf) {
     const bool mv = base + ml < nlines;
     LinePtr lp{nullptr, nullptr, 0};
     if (mv) lp = src.get(base + ml);
     if (lane < kLineWarp) {
-      snw[w][lane] = lp.nw;
-      sst[w][lane] = lp.step;
-    }
-    float2 v[kGatherPerLane];
-#pragma unroll
-    for (int k = 0; k < kGatherPerLane; ++k) {  // all loads first, then the stores
-      const int i = lane + 32 * k;
-      const int fld = i / (kLineCells * kLineWarp), c = (i / kLineWarp) % kLineCells;
-      v[k] = make_float2(0.f, 0.f);
-      if (mv && i < kGather) v[k] = fld ? lp.cur[c * lp.step] : lp.nw[c * lp.step];
+      snw[w][buf][lane] = lp.nw;
+      sst[w][buf][lane] = lp.step;
     }
 #pragma unroll
     for (int k = 0; k < kGatherPerLane; ++k) {
       const int i = lane + 32 * k;
       const int fld = i / (kLineCells * kLineWarp), c = (i / kLineWarp) % kLineCells;
-      if (i < kGather) sl[w][fld][c][ml] = v[k];
+      if (i < kGather) {
+        const float2 *from = mv ? (fld ? lp.cur : lp.nw) + c * lp.step
+                                : reinterpret_cast<const float2 *>(wc);
+        cp_async8(&sl[w][buf][fld][c][ml], from, mv);
+      }
     }
+  };
+  long long base = warp * kLineWarp;
+  if (base < nlines) gather(base, 0);
+  cp_async_commit();
+  for (int buf = 0; base < nlines; base += stride, buf ^= 1) {
+    if (base + stride < nlines) gather(base + stride, buf ^ 1);
+    cp_async_commit();
+    cp_async_wait1();  // this pass's copies have landed
     __syncwarp();
+    float2(*ls)[kLineCells][kLineWarp] = sl[w][buf];
     float f0[8], f1[8];
     {
       const int c0 = j + 2 * t, c1 = c0 + 1;
-      const float2 a0 = sl[w][0][c0][la], a1 = sl[w][0][c1][la];
-      const float2 b0 = sl[w][1][c0][la], b1 = sl[w][1][c1][la];
+      const float2 a0 = ls[0][c0][la], a1 = ls[0][c1][la];
+      const float2 b0 = ls[1][c0][la], b1 = ls[1][c1][la];
       f0[0] = a0.x, f0[1] = a1.x, f0[2] = a0.y, f0[3] = a1.y;
       f0[4] = b0.x, f0[5] = b1.x, f0[6] = b0.y, f0[7] = b1.y;
-      const float2 e0 = sl[w][0][c0][lb], e1 = sl[w][0][c1][lb];
-      const float2 h0 = sl[w][1][c0][lb], h1 = sl[w][1][c1][lb];
+      const float2 e0 = ls[0][c0][lb], e1 = ls[0][c1][lb];
+      const float2 h0 = ls[1][c0][lb], h1 = ls[1][c1][lb];
       f1[0] = e0.x, f1[1] = e1.x, f1[2] = e0.y, f1[3] = e1.y;
       f1[4] = h0.x, f1[5] = h1.x, f1[6] = h0.y, f1[7] = h1.y;
     }
@@ -712,17 +735,17 @@ __global__ void __launch_bounds__(128, 8) lb_line_kernel(const float *__restrict
     if (net16(sm, f0, f1, depth, depth, rr0, rr1, y) && t == 0) {
       // new value = stencil output + correction, rounded as the two-pass form
       if (base + la < nlines) {
-        const float2 v = sl[w][0][j][la];
-        snw[w][la][j * sst[w][la]] = make_float2(__fadd_rn(v.x, __fmul_rn(rr0, y[0])),
-                                                 __fadd_rn(v.y, __fmul_rn(rr0, y[1])));
+        const float2 v = ls[0][j][la];
+        snw[w][buf][la][j * sst[w][buf][la]] = make_float2(
+            __fadd_rn(v.x, __fmul_rn(rr0, y[0])), __fadd_rn(v.y, __fmul_rn(rr0, y[1])));
       }
       if (base + lb < nlines) {
-        const float2 v = sl[w][0][j][lb];
-        snw[w][lb][j * sst[w][lb]] = make_float2(__fadd_rn(v.x, __fmul_rn(rr1, y[2])),
-                                                 __fadd_rn(v.y, __fmul_rn(rr1, y[3])));
+        const float2 v = ls[0][j][lb];
+        snw[w][buf][lb][j * sst[w][buf][lb]] = make_float2(
+            __fadd_rn(v.x, __fmul_rn(rr1, y[2])), __fadd_rn(v.y, __fmul_rn(rr1, y[3])));
       }
     }
-    __syncwarp();  // the next pass overwrites this warp's staging
+    __syncwarp();  // the pass after next overwrites this buffer
   }
 }
 
@@ -806,6 +829,12 @@ __global__ void crop_kernel(float2 *dst, long long sx, long long sy, long long s
       v = src[(z + oz) * wplane + (y + oy) * wpitch + (x + ox)];
     dst[(z * sy + y) * pitch + x] = v;
   }
+}
+
+// The face-line pass: at most one wave of its 8 CTAs per SM (each stages
+// the weights once and loops over its passes).
+int line_grid(long long nl) {
+  return static_cast<int>(std::max<long long>(1, std::min<long long>((nl + 15) / 16, 152 * 8)));
 }
 
 int grid_for(long long n, int per_block) {
@@ -913,7 +942,7 @@ cudaError_t launch_lb_fused(cudaStream_t st, const float *wc, int layer, const i
                             long long nl, const int4 *edge, long long ne, float2 *nw,
                             const float2 *cur, long long pitch, long long plane, float2 *corr) {
   if (nl > 0) {
-    lb_line_kernel<LineSrc><<<grid_for(nl, 4 * kLineWarp), 128, 0, st>>>(
+    lb_line_kernel<LineSrc><<<line_grid(nl), 128, 0, st>>>(
         wc, LineSrc{lines, nw, cur, pitch, plane}, nl, layer);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -926,7 +955,7 @@ cudaError_t launch_lb_batch_fused(cudaStream_t st, const float *wc, int layer, c
                                   long long nl, const int4 *edge, long long ne,
                                   const LbShot *shots, int cur_buf, float2 *corr) {
   if (nl > 0) {
-    lb_line_kernel<BatchLineSrc><<<grid_for(nl, 4 * kLineWarp), 128, 0, st>>>(
+    lb_line_kernel<BatchLineSrc><<<line_grid(nl), 128, 0, st>>>(
         wc, BatchLineSrc{lines, shots, cur_buf}, nl, layer);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;

@@ -170,6 +170,7 @@ void fill_weights(StepParams *p, float dx, float dy, float dz, float dt) {
   }
   p->dt = dt;
   p->dt2 = dt * dt;
+  p->dt2_iso = static_cast<float>(static_cast<double>(p->dt2) / (static_cast<double>(dx) * dx));
 }
 
 namespace {
@@ -191,7 +192,10 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
   p.plane = s->plane;
   fill_weights(&p, dx, dy, dz, dt);
   // the FP16/BF16 medium stores the velocity terms scaled by 2^-vexp
-  if (s->coef_form == CF_F16 || s->coef_form == CF_BF16) p.dt2 = ldexpf(p.dt2, s->vexp);
+  if (s->coef_form == CF_F16 || s->coef_form == CF_BF16) {
+    p.dt2 = ldexpf(p.dt2, s->vexp);
+    p.dt2_iso = ldexpf(p.dt2_iso, s->vexp);
+  }
   const dc_device_data &a = s->handle->abi;
   p.prev = reinterpret_cast<float2 *>(a.pp);
   p.cur = reinterpret_cast<const float2 *>(a.pc);
