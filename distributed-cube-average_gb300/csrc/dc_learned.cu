@@ -634,8 +634,7 @@ struct LineSrc {  // the face lines of one simulation
   float2 *nw;
   const float2 *cur;
   long long pitch, plane;
-  __device__ __forceinline__ LinePtr get(long long l) const {
-    const int4 c = lines[l];
+  __device__ __forceinline__ LinePtr at(const int4 c) const {
     const long long g = static_cast<long long>(c.z) * plane + static_cast<long long>(c.y) * pitch + c.x;
     return LinePtr{nw + g, cur + g, inward_step(c.w, pitch, plane)};
   }
@@ -645,8 +644,7 @@ struct BatchLineSrc {  // the face lines of every shot of a batch
   const int4 *lines;
   const LbShot *shots;
   int cur_buf;
-  __device__ __forceinline__ LinePtr get(long long l) const {
-    const int4 c = lines[l];
+  __device__ __forceinline__ LinePtr at(const int4 c) const {
     const LbShot &sh = shots[c.w >> 8];
     const long long g = static_cast<long long>(c.z) * sh.plane +
                         static_cast<long long>(c.y) * sh.pitch + c.x;
@@ -666,19 +664,24 @@ __device__ __forceinline__ void cp_async8(void *sdst, const void *gsrc, bool val
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
-__device__ __forceinline__ void cp_async_wait1() {
-  asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+__device__ __forceinline__ void cp_async_wait0() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-// Each warp double-buffers its staging: the copies of the next pass are in
-// flight (cp.async, no registers held) while the network runs on this one.
+// Each warp keeps one pass's copies in flight while the network runs on
+// the previous one: at the top of pass p it waits for the group that
+// brought pass p's cells and pass p+1's line entries, then queues pass
+// p+1's cells (addresses from those entries) and pass p+2's entries.
+// Cells and entries are double-buffered in shared memory; nothing waits on
+// a global load issued in the same pass.
 template <class Src>
 __global__ void __launch_bounds__(128, 8) lb_line_kernel(const float *__restrict__ wc, Src src,
                                                          long long nlines, int layer) {
   __shared__ NetSmem sm;
   // per warp and buffer: [field][cell][line] (field 0 = new, 1 = current),
-  // and the lines' new-field pointers and strides for the writes
+  // the lines' table entries, and their new-field pointers and strides
   __shared__ __align__(16) float2 sl[4][2][2][kLineCells][kLineWarp];
+  __shared__ __align__(16) int4 sent[4][2][kLineWarp];
   __shared__ float2 *snw[4][2][kLineWarp];
   __shared__ long long sst[4][2][kLineWarp];
   stage_net(wc, sm);
@@ -690,11 +693,25 @@ __global__ void __launch_bounds__(128, 8) lb_line_kernel(const float *__restrict
   const int j = g % kLine, la = g / kLine, lb = la + 8 / kLine;
   const int depth = layer - 1 - j;
   const int ml = lane % kLineWarp;  // the line this lane copies (32 is a multiple of 4)
-  // queues the copies of the pass at `base` into buffer `buf`
-  auto gather = [&](long long base, int buf) {
+  const float2 *dummy = reinterpret_cast<const float2 *>(wc);
+  // queues the table entries of the pass at `base` into entry buffer `buf`
+  auto fetch_entries = [&](long long base, int buf) {
+    if (lane < kLineWarp) {
+      const bool v = base + lane < nlines;
+      const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(&sent[w][buf][lane]));
+      const void *from = v ? static_cast<const void *>(src.lines + base + lane)
+                           : static_cast<const void *>(wc);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(from),
+                   "r"(v ? 16 : 0)
+                   : "memory");
+    }
+  };
+  // queues the cells of the pass at `base` (entries in buffer `buf`) into
+  // cell buffer `buf`
+  auto fetch_cells = [&](long long base, int buf) {
     const bool mv = base + ml < nlines;
     LinePtr lp{nullptr, nullptr, 0};
-    if (mv) lp = src.get(base + ml);
+    if (mv) lp = src.at(sent[w][buf][ml]);
     if (lane < kLineWarp) {
       snw[w][buf][lane] = lp.nw;
       sst[w][buf][lane] = lp.step;
@@ -703,21 +720,29 @@ __global__ void __launch_bounds__(128, 8) lb_line_kernel(const float *__restrict
     for (int k = 0; k < kGatherPerLane; ++k) {
       const int i = lane + 32 * k;
       const int fld = i / (kLineCells * kLineWarp), c = (i / kLineWarp) % kLineCells;
-      if (i < kGather) {
-        const float2 *from = mv ? (fld ? lp.cur : lp.nw) + c * lp.step
-                                : reinterpret_cast<const float2 *>(wc);
-        cp_async8(&sl[w][buf][fld][c][ml], from, mv);
-      }
+      if (i < kGather)
+        cp_async8(&sl[w][buf][fld][c][ml], mv ? (fld ? lp.cur : lp.nw) + c * lp.step : dummy,
+                  mv);
     }
   };
   long long base = warp * kLineWarp;
-  if (base < nlines) gather(base, 0);
+  if (base < nlines) {
+    fetch_entries(base, 0);
+    cp_async_commit();
+    cp_async_wait0();
+    __syncwarp();
+    fetch_cells(base, 0);
+    fetch_entries(base + stride, 1);
+  }
   cp_async_commit();
   for (int buf = 0; base < nlines; base += stride, buf ^= 1) {
-    if (base + stride < nlines) gather(base + stride, buf ^ 1);
-    cp_async_commit();
-    cp_async_wait1();  // this pass's copies have landed
+    cp_async_wait0();  // this pass's cells and the next pass's entries have landed
     __syncwarp();
+    if (base + stride < nlines) {
+      fetch_cells(base + stride, buf ^ 1);
+      fetch_entries(base + 2 * stride, buf);
+    }
+    cp_async_commit();
     float2(*ls)[kLineCells][kLineWarp] = sl[w][buf];
     float f0[8], f1[8];
     {
