@@ -819,7 +819,8 @@ def run_best(args, rank, world, local):
                    "speedup_vs_plain": best / plain,
                    "accuracy": "FP16 medium: rel. L2 vs FP64 oracle 3.2e-4 (batched shot, 70 "
                                "steps) and 7.3e-4 (300 steps); learned layer: reflected energy "
-                               "6.8e-3 vs 1.3e-4 for the 48-cell sponge (384^3, 32-cell band)",
+                               "0.060 vs 0.0013 for the 48-cell sponge (384^3, 32-cell band, "
+                               "1503 steps; bench.py --form learned)",
                    "global_batch": args.shots * world, "seq_len": None,
                    "parallelism": f"shots{args.shots}x{world}",
                    "l2": "inputs ~40 GB >> 129 MB L2; no flush"},
