@@ -57,6 +57,7 @@ struct Batch {
   std::vector<BShot> shots;
   // device tables (rebuilt by prepare)
   CUtensorMap *d_maps = nullptr;
+  int *d_order = nullptr;          // work items in medium order, all groups
   float *d_sponge = nullptr, *d_src = nullptr, *d_src_pre = nullptr, *d_traces = nullptr;
   int2 *d_rec_col = nullptr;
   int *d_rec_z = nullptr, *d_rec_r = nullptr;
@@ -112,6 +113,8 @@ void drop_graphs(Batch *b) {
 
 void free_tables(Batch *b) {
   cudaFree(b->d_maps);
+  cudaFree(b->d_order);
+  b->d_order = nullptr;
   cudaFree(b->d_sponge);
   cudaFree(b->d_src);
   cudaFree(b->d_src_pre);
@@ -251,9 +254,10 @@ int prepare(Batch *b, int ty, int zsplit, bool persistent) {
   // launch parameters, one group per kMaxBatchShots shots
   StepParams common{};
   fill_weights(&common, b->dx, b->dy, b->dz, b->dt);
-  if (b->coef_form == CF_F16 || b->coef_form == CF_BF16)
+  if (b->coef_form == CF_F16 || b->coef_form == CF_BF16) {
     common.dt2 = ldexpf(common.dt2, b->vexp);
     common.dt2_iso = ldexpf(common.dt2_iso, b->vexp);
+  }
   b->groups.clear();
   long long max_items = 0;
   for (int g0 = 0; g0 < n; g0 += kMaxBatchShots) {
@@ -317,6 +321,45 @@ int prepare(Batch *b, int ty, int zsplit, bool persistent) {
     max_items = std::max(max_items, items);
     b->groups.push_back(bl);
   }
+  // Launch order: the crops overlap in the shared medium, so the items are
+  // sorted by their medium position (z-chunk, tile row, tile column, then
+  // shot).  CTAs that run together then read the same medium columns and
+  // all but the first find them in L2.  Every item writes its own outputs,
+  // so the order changes no result.
+  std::vector<int> order;
+  std::vector<size_t> group_off;
+  for (const BatchLaunch &bl : b->groups) {
+    group_off.push_back(order.size());
+    struct Key {
+      long long z, y, x;
+      int s, item;
+    };
+    std::vector<Key> keys;
+    keys.reserve(static_cast<size_t>(bl.n_items));
+    for (int s = 0; s < bl.nshots; ++s) {
+      const StepParams &p = bl.shot[s];
+      for (int local = 0; local < bl.item_prefix[s + 1] - bl.item_prefix[s]; ++local) {
+        const int ix = local % bl.tiles_x[s];
+        const int iy = (local / bl.tiles_x[s]) % bl.tiles_y[s];
+        const int iz = local / (bl.tiles_x[s] * bl.tiles_y[s]);
+        const long long mx = p.mox + p.tile_x0 + 32ll * ix, my = p.moy + p.tile_y0 + ty * iy;
+        const long long mz = p.moz + p.z0 + static_cast<long long>(iz) * p.zchunk;
+        keys.push_back(Key{mz / std::max(1, p.zchunk), my / ty, mx / 32, s,
+                           bl.item_prefix[s] + local});
+      }
+    }
+    std::stable_sort(keys.begin(), keys.end(), [](const Key &a, const Key &c) {
+      if (a.z != c.z) return a.z < c.z;
+      if (a.y != c.y) return a.y < c.y;
+      if (a.x != c.x) return a.x < c.x;
+      return a.s < c.s;
+    });
+    for (const Key &k : keys) order.push_back(k.item);
+  }
+  BATCH_TRY(cudaMalloc(&b->d_order, sizeof(int) * std::max<size_t>(order.size(), 1)));
+  BATCH_TRY(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * order.size(),
+                            cudaMemcpyHostToDevice, b->stream));
+  for (size_t g = 0; g < b->groups.size(); ++g) b->groups[g].order = b->d_order + group_off[g];
   BATCH_TRY(batch_prepare(ty, b->coef_form));
   const bool iso = b->dx == b->dy && b->dy == b->dz;
   const int per_sm = batch_blocks_per_sm(ty, b->coef_form, iso);

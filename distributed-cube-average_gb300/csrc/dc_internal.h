@@ -111,6 +111,7 @@ constexpr int kMaxBatchShots = 64;
 struct BatchLaunch {
   CUtensorMap tm_l, tm_o1, tm_o2;  // shared medium (coefficient groups)
   const CUtensorMap *maps;          // [shot][4]: halo of buffer 0, 1; own tile of buffer 0, 1
+  const int *order;                 // launch order of the work items (null: shot by shot)
   int nshots;
   int cur_buf;                      // buffer holding (pc, qc) in every shot
   int n_items;

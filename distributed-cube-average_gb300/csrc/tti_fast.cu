@@ -558,7 +558,8 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     if (threadIdx.x == 0) atomicOr(bl.err, kErrAlign);
     return;
   }
-  for (int item = blockIdx.x; item < bl.n_items; item += gridDim.x) {
+  for (int slot = blockIdx.x; slot < bl.n_items; slot += gridDim.x) {
+    const int item = bl.order ? bl.order[slot] : slot;
     int s = 0;
     while (s + 1 < bl.nshots && bl.item_prefix[s + 1] <= item) ++s;
     const StepParams &prm = bl.shot[s];
