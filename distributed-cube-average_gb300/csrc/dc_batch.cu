@@ -68,6 +68,7 @@ struct Batch {
   bool prepared = false;
   int ty = 8, zsplit = 1;
   bool persistent = true;  // persistent CTAs, or one CTA per work item
+  bool sponge = true;      // some shot's sponge profile differs from 1
   int steps_done = 0;
   int src_applied_step = -1;
   long launches = 0;
@@ -360,9 +361,10 @@ int prepare(Batch *b, int ty, int zsplit, bool persistent) {
   BATCH_TRY(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * order.size(),
                             cudaMemcpyHostToDevice, b->stream));
   for (size_t g = 0; g < b->groups.size(); ++g) b->groups[g].order = b->d_order + group_off[g];
+  b->sponge = std::any_of(sponge.begin(), sponge.end(), [](float g) { return g != 1.0f; });
   BATCH_TRY(batch_prepare(ty, b->coef_form));
   const bool iso = b->dx == b->dy && b->dy == b->dz;
-  const int per_sm = batch_blocks_per_sm(ty, b->coef_form, iso);
+  const int per_sm = batch_blocks_per_sm(ty, b->coef_form, iso, b->sponge);
   if (per_sm < 1) return fail(DC_GB300_ERR_CUDA, "batch kernel does not fit an SM");
   int sms = 0;
   BATCH_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
@@ -385,7 +387,8 @@ cudaError_t queue_launches(Batch *b, int cur, int j) {
       bl.shot[k].prev = b->shots[g * kMaxBatchShots + k].pq[1 - cur];  // written in place
     }
     ++b->launches;
-    const cudaError_t e = launch_batch(b->stream, bl, b->ty, b->coef_form, iso, b->blocks);
+    const cudaError_t e =
+        launch_batch(b->stream, bl, b->ty, b->coef_form, iso, b->sponge, b->blocks);
     if (e != cudaSuccess) return e;
   }
   if (b->lb_cells > 0) {  // learned layer of every shot, after all stencil launches

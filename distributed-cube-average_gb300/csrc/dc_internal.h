@@ -203,9 +203,10 @@ bool fast_encode_medium_maps(int form, const float *coef, const void *coef16, co
                              long long count, int ty, CUtensorMap out[3], std::string *err);
 // Batched fast kernel (always with the sponge).  `blocks` = persistent CTAs.
 cudaError_t batch_prepare(int ty, int form);  // shared-memory attributes
-int batch_blocks_per_sm(int ty, int form, bool iso);
+// `sponge` false: every shot's sponge profile is 1 (the no-sponge sweep)
+int batch_blocks_per_sm(int ty, int form, bool iso, bool sponge);
 cudaError_t launch_batch(cudaStream_t st, const BatchLaunch &bl, int ty, int form, bool iso,
-                         int blocks);
+                         bool sponge, int blocks);
 
 // Launchers.  Return the cudaError_t of the launch.
 cudaError_t launch_fast(Sim *sim, const StepParams &prm, int cur_buf,

@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
 // (shot by shot: x tile fastest, then y tile, then z-chunk).  The shot of an
 // item is found from the per-shot prefix counts, so every index here is
 // CTA-uniform.
-template <int TX, int TY, int CF, bool ISO>
+template <int TX, int TY, int CF, bool SPONGE, bool ISO>
 __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     batch_kernel(const __grid_constant__ BatchLaunch bl) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -574,7 +574,7 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
     const CUtensorMap *m = bl.maps + 4 * s;
     // weights, dt2 and energy (none) are the same in every shot: read them
     // from shot 0 at fixed offsets
-    if (!sweep_column<TX, TY, CF, true, ISO>(m + bl.cur_buf, m + 2 + (1 - bl.cur_buf),
+    if (!sweep_column<TX, TY, CF, SPONGE, ISO>(m + bl.cur_buf, m + 2 + (1 - bl.cur_buf),
                                              &bl.tm_l, &bl.tm_o1, &bl.tm_o2, prm, bl.shot[0],
                                              x0, y0, zb, ze, smem))
       return;
@@ -743,17 +743,26 @@ bool fast_encode_maps(Sim *sim, std::string *err) {
 
 namespace {
 
-template <int TY, int CF, bool ISO>
+// Batch kernel variants: every coefficient form and spacing with the
+// sponge; without it (all shots' profiles are 1, e.g. learned layers) for
+// equal spacing and the FP32 / FP16 / BF16 forms.
+template <int CF>
+constexpr bool kNoSpongeForm = CF == CF_F32 || CF == CF_F16 || CF == CF_BF16;
+
+template <int TY, int CF, bool SPONGE, bool ISO>
 cudaError_t batch_attr() {
-  return cudaFuncSetAttribute(batch_kernel<kTX, TY, CF, ISO>,
+  return cudaFuncSetAttribute(batch_kernel<kTX, TY, CF, SPONGE, ISO>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               FastLayout<kTX, TY, CF>::SMEM_BYTES);
 }
 
 template <int TY, int CF>
 cudaError_t batch_attr_cf() {
-  cudaError_t e = batch_attr<TY, CF, false>();
-  return e == cudaSuccess ? batch_attr<TY, CF, true>() : e;
+  cudaError_t e = batch_attr<TY, CF, true, false>();
+  if (e == cudaSuccess) e = batch_attr<TY, CF, true, true>();
+  if constexpr (kNoSpongeForm<CF>)
+    if (e == cudaSuccess) e = batch_attr<TY, CF, false, true>();
+  return e;
 }
 
 template <int TY>
@@ -766,10 +775,11 @@ cudaError_t batch_attr_ty(int form) {
   }
 }
 
-template <int TY, int CF, bool ISO>
+template <int TY, int CF, bool SPONGE, bool ISO>
 int batch_occ() {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<kTX, TY, CF, ISO>, kTX * TY,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<kTX, TY, CF, SPONGE, ISO>,
+                                                    kTX * TY,
                                                     FastLayout<kTX, TY, CF>::SMEM_BYTES) !=
       cudaSuccess)
     return 0;
@@ -777,38 +787,49 @@ int batch_occ() {
 }
 
 template <int TY, int CF>
-int batch_occ_cf(bool iso) {
-  return iso ? batch_occ<TY, CF, true>() : batch_occ<TY, CF, false>();
+int batch_occ_cf(bool iso, bool sponge) {
+  if constexpr (kNoSpongeForm<CF>)
+    if (iso && !sponge) return batch_occ<TY, CF, false, true>();
+  return iso ? batch_occ<TY, CF, true, true>() : batch_occ<TY, CF, true, false>();
 }
 
 template <int TY>
-int batch_occ_ty(int form, bool iso) {
+int batch_occ_ty(int form, bool iso, bool sponge) {
   switch (form) {
-    case CF_F16: return batch_occ_cf<TY, CF_F16>(iso);
-    case CF_BF16: return batch_occ_cf<TY, CF_BF16>(iso);
-    case CF_VV: return batch_occ_cf<TY, CF_VV>(iso);
-    default: return batch_occ_cf<TY, CF_F32>(iso);
+    case CF_F16: return batch_occ_cf<TY, CF_F16>(iso, sponge);
+    case CF_BF16: return batch_occ_cf<TY, CF_BF16>(iso, sponge);
+    case CF_VV: return batch_occ_cf<TY, CF_VV>(iso, sponge);
+    default: return batch_occ_cf<TY, CF_F32>(iso, sponge);
   }
 }
 
 template <int TY, int CF>
-cudaError_t launch_batch_cf(cudaStream_t st, const BatchLaunch &bl, bool iso, int blocks) {
+cudaError_t launch_batch_cf(cudaStream_t st, const BatchLaunch &bl, bool iso, bool sponge,
+                            int blocks) {
   const int smem = FastLayout<kTX, TY, CF>::SMEM_BYTES;
-  if (iso)
-    batch_kernel<kTX, TY, CF, true><<<blocks, kTX * TY, smem, st>>>(bl);
-  else
-    batch_kernel<kTX, TY, CF, false><<<blocks, kTX * TY, smem, st>>>(bl);
+  bool done = false;
+  if constexpr (kNoSpongeForm<CF>)
+    if (iso && !sponge) {
+      batch_kernel<kTX, TY, CF, false, true><<<blocks, kTX * TY, smem, st>>>(bl);
+      done = true;
+    }
+  if (!done) {
+    if (iso)
+      batch_kernel<kTX, TY, CF, true, true><<<blocks, kTX * TY, smem, st>>>(bl);
+    else
+      batch_kernel<kTX, TY, CF, true, false><<<blocks, kTX * TY, smem, st>>>(bl);
+  }
   return cudaGetLastError();
 }
 
 template <int TY>
 cudaError_t launch_batch_ty(cudaStream_t st, const BatchLaunch &bl, int form, bool iso,
-                            int blocks) {
+                            bool sponge, int blocks) {
   switch (form) {
-    case CF_F16: return launch_batch_cf<TY, CF_F16>(st, bl, iso, blocks);
-    case CF_BF16: return launch_batch_cf<TY, CF_BF16>(st, bl, iso, blocks);
-    case CF_VV: return launch_batch_cf<TY, CF_VV>(st, bl, iso, blocks);
-    default: return launch_batch_cf<TY, CF_F32>(st, bl, iso, blocks);
+    case CF_F16: return launch_batch_cf<TY, CF_F16>(st, bl, iso, sponge, blocks);
+    case CF_BF16: return launch_batch_cf<TY, CF_BF16>(st, bl, iso, sponge, blocks);
+    case CF_VV: return launch_batch_cf<TY, CF_VV>(st, bl, iso, sponge, blocks);
+    default: return launch_batch_cf<TY, CF_F32>(st, bl, iso, sponge, blocks);
   }
 }
 
@@ -818,14 +839,14 @@ cudaError_t batch_prepare(int ty, int form) {
   return ty == 16 ? batch_attr_ty<16>(form) : batch_attr_ty<8>(form);
 }
 
-int batch_blocks_per_sm(int ty, int form, bool iso) {
-  return ty == 16 ? batch_occ_ty<16>(form, iso) : batch_occ_ty<8>(form, iso);
+int batch_blocks_per_sm(int ty, int form, bool iso, bool sponge) {
+  return ty == 16 ? batch_occ_ty<16>(form, iso, sponge) : batch_occ_ty<8>(form, iso, sponge);
 }
 
 cudaError_t launch_batch(cudaStream_t st, const BatchLaunch &bl, int ty, int form, bool iso,
-                         int blocks) {
-  return ty == 16 ? launch_batch_ty<16>(st, bl, form, iso, blocks)
-                  : launch_batch_ty<8>(st, bl, form, iso, blocks);
+                         bool sponge, int blocks) {
+  return ty == 16 ? launch_batch_ty<16>(st, bl, form, iso, sponge, blocks)
+                  : launch_batch_ty<8>(st, bl, form, iso, sponge, blocks);
 }
 
 cudaError_t launch_fast(Sim *sim, const StepParams &prm, int cur_buf, int prev_buf) {
