@@ -138,9 +138,9 @@ constexpr float kL1 = 4.0f / 5.0f, kL2 = -1.0f / 5.0f, kL3 = 4.0f / 105.0f,
 
 // Two forms of each derivative with the constant weights: two FMA chains
 // summed at the end (shorter dependency chains), or one chain (one
-// instruction fewer).  The FP32-medium sweep, nearer its memory bound, runs
-// faster with the first, the FP16/BF16 sweeps with the second (616^3 FP32:
-// 2.942 vs 2.975 ms; 64-shot FP16 batch: 33.19 vs 32.57 ms).
+// instruction fewer).  The FP16/BF16 sweeps run 2 % faster with the second
+// (64-shot FP16 batch: 32.57 vs 33.19 ms); the FP32-medium sweep, nearer its
+// memory bound, gains nothing from it and keeps the first.
 template <bool CHAIN>
 __device__ __forceinline__ float2 d2k(float2 c, float2 m1, float2 p1, float2 m2, float2 p2,
                                       float2 m3, float2 p3, float2 m4, float2 p4) {
