@@ -21,6 +21,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "dc_internal.h"
@@ -76,19 +77,49 @@ struct Batch {
   // learned thin layer on every shot (after each step's stencil launches)
   const float *lb_params = nullptr;
   int lb_layer = 0;
-  int4 *d_lb_lines = nullptr;  // face lines (meta bits 8..31: the shot)
-  int4 *d_lb_cells = nullptr;  // edge cells
-  float2 *d_lb_corr = nullptr;
+  // With the layer, the shots split into two halves, each its own chain of
+  // launches in the step graph (stencil, then its layer), so one half's
+  // network overlaps the other half's stencil.
+  struct LbBranch {
+    int4 *d_lines = nullptr;   // face lines (meta bits 8..31: the shot)
+    int4 *d_edge = nullptr;    // edge cells
+    float2 *d_corr = nullptr;  // edge-cell corrections
+    long long nl = 0, ne = 0;
+  } lb[2];
   LbShot *d_lb_shots = nullptr;
   long long lb_cells = 0;      // corrected cells in all (0: no layer)
-  long long lb_lines = 0, lb_edge = 0;
+  int nbranch = 1;             // launch chains per step (2 with the layer and >= 2 shots)
+  std::vector<int> group_first, group_branch;  // per launch group: first shot, chain
+  cudaStream_t side = nullptr;                 // the second chain's stream
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 // Learned-layer launches of one step: the face-line pass, then the edge
 // cells' network and add.
 long lb_launches(const Batch *b) {
   if (b->lb_cells <= 0) return 0;
-  return (b->lb_lines > 0 ? 1 : 0) + (b->lb_edge > 0 ? 2 : 0);
+  long n = 0;
+  for (int br = 0; br < b->nbranch; ++br)
+    n += (b->lb[br].nl > 0 ? 1 : 0) + (b->lb[br].ne > 0 ? 2 : 0);
+  return n;
+}
+
+// The launch chain of shot k.
+int branch_of(const Batch *b, size_t k) {
+  return b->nbranch == 2 && k >= (b->shots.size() + 1) / 2 ? 1 : 0;
+}
+
+void free_layer(Batch *b) {
+  for (auto &l : b->lb) {
+    cudaFree(l.d_lines);
+    cudaFree(l.d_edge);
+    cudaFree(l.d_corr);
+    l = Batch::LbBranch{};
+  }
+  cudaFree(b->d_lb_shots);
+  b->d_lb_shots = nullptr;
+  b->lb_cells = 0;
+  b->nbranch = 1;
 }
 
 int fail(int code, const std::string &msg) {
@@ -138,10 +169,10 @@ void release(Batch *b) {
     cudaFree(s.pq[0]);
     cudaFree(s.pq[1]);
   }
-  cudaFree(b->d_lb_lines);
-  cudaFree(b->d_lb_cells);
-  cudaFree(b->d_lb_corr);
-  cudaFree(b->d_lb_shots);
+  free_layer(b);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
+  if (b->side) cudaStreamDestroy(b->side);
   cudaFree(b->coef);
   cudaFree(b->coef16);
   cudaFree(b->d_step);
@@ -260,15 +291,32 @@ int prepare(Batch *b, int ty, int zsplit, bool persistent) {
     common.dt2_iso = ldexpf(common.dt2_iso, b->vexp);
   }
   b->groups.clear();
+  b->group_first.clear();
+  b->group_branch.clear();
   long long max_items = 0;
-  for (int g0 = 0; g0 < n; g0 += kMaxBatchShots) {
+  // launch groups of up to kMaxBatchShots shots, never spanning two chains
+  std::vector<std::pair<int, int>> spans;  // [first, last) shots
+  for (int br = 0; br < b->nbranch; ++br) {
+    int lo = 0, hi = n;
+    if (b->nbranch == 2) {
+      lo = br == 0 ? 0 : (n + 1) / 2;
+      hi = br == 0 ? (n + 1) / 2 : n;
+    }
+    for (int g0 = lo; g0 < hi; g0 += kMaxBatchShots) {
+      spans.emplace_back(g0, std::min(hi, g0 + kMaxBatchShots));
+      b->group_branch.push_back(br);
+    }
+  }
+  for (const auto &span : spans) {
+    const int g0 = span.first;
     BatchLaunch bl;
     std::memset(&bl, 0, sizeof(bl));
     bl.tm_l = tm_c[0];
     bl.tm_o1 = tm_c[1];
     bl.tm_o2 = tm_c[2];
     bl.maps = b->d_maps + 4 * g0;
-    bl.nshots = std::min(kMaxBatchShots, n - g0);
+    bl.nshots = span.second - g0;
+    b->group_first.push_back(g0);
     bl.err = b->d_err;
     long long items = 0;
     for (int k = 0; k < bl.nshots; ++k) {
@@ -377,27 +425,50 @@ int prepare(Batch *b, int ty, int zsplit, bool persistent) {
 
 // Queues one step of every shot with (pc, qc) in buffer `cur`, the j-th
 // step of a sequence (step = *d_step + j).
-cudaError_t queue_launches(Batch *b, int cur, int j) {
+// Queues one step of the shots of chain `br` on stream `st`.
+cudaError_t queue_chain(Batch *b, int cur, int j, int br, cudaStream_t st) {
   const bool iso = b->dx == b->dy && b->dy == b->dz;
   for (size_t g = 0; g < b->groups.size(); ++g) {
+    if (b->group_branch[g] != br) continue;
     BatchLaunch &bl = b->groups[g];
     bl.cur_buf = cur;
     for (int k = 0; k < bl.nshots; ++k) {
       bl.shot[k].step_offset = j;
-      bl.shot[k].prev = b->shots[g * kMaxBatchShots + k].pq[1 - cur];  // written in place
+      bl.shot[k].prev = b->shots[b->group_first[g] + k].pq[1 - cur];  // written in place
     }
     ++b->launches;
-    const cudaError_t e =
-        launch_batch(b->stream, bl, b->ty, b->coef_form, iso, b->sponge, b->blocks);
+    const cudaError_t e = launch_batch(st, bl, b->ty, b->coef_form, iso, b->sponge, b->blocks);
     if (e != cudaSuccess) return e;
   }
-  if (b->lb_cells > 0) {  // learned layer of every shot, after all stencil launches
-    b->launches += lb_launches(b);
-    return launch_lb_batch_fused(b->stream, b->lb_params, b->lb_layer, b->d_lb_lines,
-                                 b->lb_lines, b->d_lb_cells, b->lb_edge, b->d_lb_shots, cur,
-                                 b->d_lb_corr);
+  if (b->lb_cells > 0) {  // the chain's learned layers, after its stencil launches
+    const Batch::LbBranch &l = b->lb[br];
+    b->launches += (l.nl > 0 ? 1 : 0) + (l.ne > 0 ? 2 : 0);
+    return launch_lb_batch_fused(st, b->lb_params, b->lb_layer, l.d_lines, l.nl, l.d_edge, l.ne,
+                                 b->d_lb_shots, cur, l.d_corr);
   }
   return cudaSuccess;
+}
+
+// Queues `steps` steps, the first with (pc, qc) in buffer `cur0`: with two
+// chains the side stream forks from the batch stream and joins it again at
+// the end.
+cudaError_t queue_steps(Batch *b, int cur0, int steps) {
+  if (b->nbranch == 1) {
+    for (int j = 0; j < steps; ++j) {
+      const cudaError_t e = queue_chain(b, (cur0 + j) & 1, j, 0, b->stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaEventRecord(b->ev_fork, b->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, b->ev_fork, 0);
+  for (int j = 0; j < steps && e == cudaSuccess; ++j) {
+    e = queue_chain(b, (cur0 + j) & 1, j, 0, b->stream);
+    if (e == cudaSuccess) e = queue_chain(b, (cur0 + j) & 1, j, 1, b->side);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(b->ev_join, b->side);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_join, 0);
+  return e;
 }
 
 bool source_pending(const Batch *b) {
@@ -455,8 +526,7 @@ int run_steps(Batch *b, int steps) {
       BATCH_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
       const long before = b->launches;
       cudaError_t e = cudaSuccess;
-      for (int j = 0; j < kGraphSteps && e == cudaSuccess; ++j)
-        e = queue_launches(b, (cur + j) & 1, j);
+      e = queue_steps(b, cur, kGraphSteps);
       if (e == cudaSuccess) e = launch_advance_step(b->stream, b->d_step, kGraphSteps);
       const cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
       b->launches = before;
@@ -476,7 +546,7 @@ int run_steps(Batch *b, int steps) {
     left -= kGraphSteps;
     b->steps_done += kGraphSteps;
   }
-  for (int j = 0; j < left; ++j) BATCH_TRY(queue_launches(b, (b->steps_done + j) & 1, j));
+  if (left > 0) BATCH_TRY(queue_steps(b, b->steps_done & 1, left));
   if (left > 0) {
     ++b->launches;
     BATCH_TRY(launch_advance_step(b->stream, b->d_step, left));
@@ -740,56 +810,57 @@ extern "C" int dc_gb300_batch_set_learned_layer(dc_gb300_batch *h, const dc_gb30
   BATCH_TRY(cudaSetDevice(b->device));
   BATCH_TRY(cudaStreamSynchronize(b->stream));
   dcg::drop_graphs(b);
-  cudaFree(b->d_lb_lines);
-  cudaFree(b->d_lb_cells);
-  cudaFree(b->d_lb_corr);
-  cudaFree(b->d_lb_shots);
-  b->d_lb_lines = nullptr;
-  b->d_lb_cells = nullptr;
-  b->d_lb_corr = nullptr;
-  b->d_lb_shots = nullptr;
-  b->lb_cells = b->lb_lines = b->lb_edge = 0;
+  dcg::free_layer(b);
+  b->prepared = false;  // the launch groups follow the chains
   b->lb_layer = 0;
   b->lb_params = nullptr;
   if (layer == 0) return DC_GB300_OK;
   if (b->shots.size() > (1u << 23)) return fail(DC_GB300_ERR_ARG, "too many shots");
-  std::vector<int4> lines, edge;
+  if (b->shots.size() >= 2) {
+    if (!b->side) BATCH_TRY(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+    if (!b->ev_fork) BATCH_TRY(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+    if (!b->ev_join) BATCH_TRY(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+    b->nbranch = 2;
+  }
+  std::vector<int4> lines[2], edge[2];
   std::vector<dcg::LbShot> tab;
   long long total = 0;
   for (size_t k = 0; k < b->shots.size(); ++k) {
+    const int br = dcg::branch_of(b, k);
     const dcg::BShot &s = b->shots[k];
     if (s.cfg.sx < 2 * layer + 16 || s.cfg.sy < 2 * layer + 16 || s.cfg.sz < 2 * layer + 16)
       return fail(DC_GB300_ERR_ARG, "every shot's interior must keep at least 8 cells per axis");
     const dcg::LayerPlan plan = dcg::layer_plan(s.cfg.sx, s.cfg.sy, s.cfg.sz, layer);
     for (int4 v : plan.lines) {
       v.w |= static_cast<int>(k) << 8;
-      lines.push_back(v);
+      lines[br].push_back(v);
     }
     for (int4 v : plan.edge) {
       v.w |= static_cast<int>(k) << 8;
-      edge.push_back(v);
+      edge[br].push_back(v);
     }
     total += static_cast<long long>(dcg::layer_cells(s.cfg.sx, s.cfg.sy, s.cfg.sz, layer).size());
     tab.push_back(dcg::LbShot{{s.pq[0], s.pq[1]}, s.pitch, s.plane});
   }
-  const long long nl = static_cast<long long>(lines.size());
-  const long long ne = static_cast<long long>(edge.size());
-  BATCH_TRY(cudaMalloc(&b->d_lb_lines, sizeof(int4) * std::max(nl, 1LL)));
-  BATCH_TRY(cudaMalloc(&b->d_lb_cells, sizeof(int4) * std::max(ne, 1LL)));
-  BATCH_TRY(cudaMalloc(&b->d_lb_corr, sizeof(float2) * std::max(ne, 1LL)));
+  for (int br = 0; br < b->nbranch; ++br) {
+    Batch::LbBranch &l = b->lb[br];
+    l.nl = static_cast<long long>(lines[br].size());
+    l.ne = static_cast<long long>(edge[br].size());
+    BATCH_TRY(cudaMalloc(&l.d_lines, sizeof(int4) * std::max(l.nl, 1LL)));
+    BATCH_TRY(cudaMalloc(&l.d_edge, sizeof(int4) * std::max(l.ne, 1LL)));
+    BATCH_TRY(cudaMalloc(&l.d_corr, sizeof(float2) * std::max(l.ne, 1LL)));
+    if (l.nl > 0)
+      BATCH_TRY(cudaMemcpyAsync(l.d_lines, lines[br].data(), sizeof(int4) * l.nl,
+                                cudaMemcpyHostToDevice, b->stream));
+    if (l.ne > 0)
+      BATCH_TRY(cudaMemcpyAsync(l.d_edge, edge[br].data(), sizeof(int4) * l.ne,
+                                cudaMemcpyHostToDevice, b->stream));
+  }
   BATCH_TRY(cudaMalloc(&b->d_lb_shots, sizeof(dcg::LbShot) * tab.size()));
-  if (nl > 0)
-    BATCH_TRY(cudaMemcpyAsync(b->d_lb_lines, lines.data(), sizeof(int4) * nl,
-                              cudaMemcpyHostToDevice, b->stream));
-  if (ne > 0)
-    BATCH_TRY(cudaMemcpyAsync(b->d_lb_cells, edge.data(), sizeof(int4) * ne,
-                              cudaMemcpyHostToDevice, b->stream));
   BATCH_TRY(cudaMemcpyAsync(b->d_lb_shots, tab.data(), sizeof(dcg::LbShot) * tab.size(),
                             cudaMemcpyHostToDevice, b->stream));
   BATCH_TRY(cudaStreamSynchronize(b->stream));
   b->lb_cells = total;
-  b->lb_lines = nl;
-  b->lb_edge = ne;
   b->lb_layer = layer;
   b->lb_params = dc_gb300_mlp_device_params(mlp);
   return DC_GB300_OK;
@@ -831,9 +902,9 @@ extern "C" int dc_gb300_batch_autotune(dc_gb300_batch *h, int steps, int *ty_out
       rc = dcg::reset_state(b);
       if (rc != DC_GB300_OK) break;
       // one untimed step (first use of this configuration), then timed ones
-      cudaError_t e = dcg::queue_launches(b, 0, 0);
+      cudaError_t e = dcg::queue_steps(b, 0, 1);
       if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
-      for (int j = 1; j <= steps && e == cudaSuccess; ++j) e = dcg::queue_launches(b, j & 1, j);
+      if (e == cudaSuccess) e = dcg::queue_steps(b, 1, steps);
       if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
       if (e == cudaSuccess) e = cudaEventSynchronize(e1);
       float ms = 0.0f;
