@@ -13,6 +13,9 @@ persistent batch kernel.
   medium box) and within 1.5e-3 of the FP64 oracle.
 * dc_gb300_batch_autotune returns one of its candidates and leaves the batch
   at step 0 with zero wavefields.
+* 130 shots span several launch groups (64 shots each), and with the
+  learned layer two launch chains: the shots at every group boundary match
+  single-shot simulations bit for bit.
 """
 import math
 
@@ -227,3 +230,50 @@ def test_batch_learned_layer_matches_single_simulation(dc, medium_coef):
                 want = sim.get_fields()
             assert np.array_equal(g["pc"], want["pc"]) and np.array_equal(g["qc"], want["qc"])
             assert np.abs(g["pc"]).max() > 0
+
+
+def test_batch_many_shots_span_launch_groups(dc, medium_coef):
+    """130 small shots: the kernel parameters hold 64 shots per launch, and
+    with the learned layer the batch runs as two launch chains of 65 shots
+    (groups of 64 + 1 each).  The shots at every group boundary match a
+    single-shot simulation bit for bit, with and without the layer."""
+    from dc_gb300 import learned
+    layer, steps, n = 8, 40, 130
+    rng = np.random.default_rng(77)
+    shots = []
+    for _ in range(n):
+        sizes = (32, 32, 32)
+        origin = (4 * int(rng.integers(0, (MEDIUM[0] - 32) // 4 + 1)),
+                  int(rng.integers(0, MEDIUM[1] - 32 + 1)), int(rng.integers(0, MEDIUM[2] - 32 + 1)))
+        src = (16, 16, 14)
+        shots.append((sizes, origin, src, 50.0))
+    check = [0, 63, 64, 65, 128, 129]
+    params = np.load(learned.WEIGHTS)
+    with dc.MLP(device=0, params=params) as mlp:
+        for with_layer in (False, True):
+            with dc.Batch(MEDIUM, D, DT, device=0, max_steps=steps + 2) as b:
+                b.set_precomp(medium_coef)
+                for sizes, origin, src, fcut in shots:
+                    b.add_shot(sizes, origin, src, fcut, 0 if with_layer else ABSORB,
+                               0.0 if with_layer else KAPPA)
+                if with_layer:
+                    b.set_learned_layer(mlp, layer)
+                b.run(steps)
+                b.synchronize()
+                got = {i: b.get_fields(i) for i in check}
+            for i in check:
+                sizes, origin, src, fcut = shots[i]
+                with dc.Simulation(sizes, D, DT, kernel=dc.KERNEL_FAST, device=0) as sim:
+                    sim.set_precomp([crop(c, origin, sizes) for c in medium_coef])
+                    sim.set_fields()
+                    sim.set_source(dense_index(sizes, src), wavelet(dc, fcut, steps + 3))
+                    if with_layer:
+                        dc.set_learned_layer(sim, mlp, layer)
+                    else:
+                        sim.set_sponge(*sponge(dc, sizes))
+                    sim.run(steps)
+                    sim.synchronize()
+                    want = sim.get_fields()
+                for k in ("pc", "qc", "pp", "qp"):
+                    assert np.array_equal(got[i][k], want[k]), (with_layer, i, k)
+                assert np.abs(got[i]["pc"]).max() > 0
