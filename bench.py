@@ -845,16 +845,20 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
-    if args.form == "batched":
-        run_batched(args, rank, world, local)
-        return
-    if args.form == "learned":
-        run_learned(args, rank, world, local)
-        return
-    if args.form == "best":
-        run_best(args, rank, world, local)
-        return
-    run_ours(args, rank, world, local)
+    try:
+        if args.form == "batched":
+            run_batched(args, rank, world, local)
+        elif args.form == "learned":
+            run_learned(args, rank, world, local)
+        elif args.form == "best":
+            run_best(args, rank, world, local)
+        else:
+            run_ours(args, rank, world, local)
+    finally:
+        if world > 1:  # ranks leave the process group together
+            import torch.distributed as dist
+            if dist.is_initialized():
+                dist.destroy_process_group()
 
 
 if __name__ == "__main__":
