@@ -475,21 +475,6 @@ bool source_pending(const Batch *b) {
   return b->steps_done > 0 && b->src_applied_step == b->steps_done;
 }
 
-// Puts the values before the fused injection back at every shot's source
-// point; the next run adds the amplitude again before its first step.
-cudaError_t settle_sources(Batch *b) {
-  if (!source_pending(b)) return cudaSuccess;
-  const int cur = b->steps_done & 1;
-  for (size_t i = 0; i < b->shots.size(); ++i) {
-    const cudaError_t e =
-        cudaMemcpyAsync(b->shots[i].pq[cur] + b->shots[i].src_gi, b->d_src_pre + 2 * i,
-                        sizeof(float2), cudaMemcpyDeviceToDevice, b->stream);
-    if (e != cudaSuccess) return e;
-  }
-  b->src_applied_step = -1;
-  return cudaSuccess;
-}
-
 int check_err(Batch *b) {
   int h = 0;
   BATCH_TRY(cudaMemcpyAsync(&h, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
