@@ -20,8 +20,9 @@ reference-facing C ABI with host buffers (dc_device_data_init with the
 copies, dc_device_add_source + dc_propagate + dc_device_swap_arrays per
 step, dc_device_data_get_results), wall clock.  ``roofline`` compares the
 stencil kernel's algorithmic bytes (64 B per update) per launch time with the
-measured HBM copy bandwidth; ``cpu_baseline`` times the CPU oracle on a
-bounded slab of the same workload.
+measured HBM copy bandwidth; ``cpu_baseline`` times the reference's own
+OpenMP path (built from its sources with its own flags) on a bounded y-slab
+of the same workload.
 
 Batched form (--form batched): 64 shots over one shared seeded medium of
 768 x 768 x 512 cells (plus a 52-cell margin per side for the shots'
@@ -55,9 +56,15 @@ each: its step cost does not change).  ``value`` is
 interior shot-point-updates per second (crop points x steps / time) of the
 best form; the line carries the plain form's rate and the ratio.
 
+Reference-CUDA form (--form refcuda): the reference's own GPU path
+(src/cuda_propagate.cu, src/device_data.cu, nvcc sm_103a) against ours on
+the same GPU and inputs (the reference's default medium and random velocity
+boundary on the plain workload's geometry).
+
 Reference arm (--impl reference): the reference's CPU implementation of the
-path (the oracle port of src/openmp_propagate.c, all host threads) on the
-same workload; each step is one time step of a 608 x 608 x 16 slab.
+path (src/openmp_propagate.c built with the reference's flags, all host
+threads; the oracle port only where the reference's sources are absent) on
+the same workload; each step is one time step of a 608 x 16 x 608 y-slab.
 """
 from __future__ import annotations
 
@@ -85,7 +92,7 @@ SRC_DEPTH = 20        # interior-relative depth of the source (cells)
 MEDIUM_SEED = 2026
 SPONGE_KAPPA = 0.35
 BYTES_PER_UPDATE = 64  # pc,qc,pp,qp + 10 coefficients read, pp,qp written
-SLAB_PLANES = 16       # CPU sample: planes per step
+SLAB_ROWS = 16         # CPU sample: updated y rows per step
 # batched form
 BATCH_MODEL = (768, 768, 512)
 BATCH_PAD = ABSORB + 4  # sponge + halo around every crop
@@ -110,7 +117,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_INTERIOR, help="interior cells per axis")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--form", choices=("plain", "mixed", "batched", "learned", "best"),
+    ap.add_argument("--form", choices=("plain", "mixed", "batched", "learned", "best",
+                                       "refcuda"),
                     default="plain")
     ap.add_argument("--shots", type=int, default=BATCH_SHOTS)
     ap.add_argument("--model", type=int, nargs=3, default=list(BATCH_MODEL),
@@ -124,7 +132,7 @@ def parse():
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"batched": 1000, "learned": 1500, "best": 1000,
-                      "mixed": 1500}.get(args.form, 2000)
+                      "mixed": 1500, "refcuda": 20}.get(args.form, 2000)
     if args.form == "mixed":
         # the mixed-precision workload: 1024 x 1024 x 768 interior + 48-cell
         # sponge, FP16 medium unless another storage is asked for
@@ -260,26 +268,29 @@ def make_spec(geom):
     return medium.layered_spec(MEDIUM_SEED, geom.sizes)
 
 
-def slab_inputs(dc, port, geom, planes: int):
-    """Host inputs of a CPU sample: a z-slab of the workload (full x-y
-    extent, `planes` updated planes around the source depth) with its medium
-    precomputed like the reference (src/precomp.c:85-105)."""
+def slab_inputs(dc, port, geom, rows: int):
+    """Host inputs of a CPU sample: a y-slab of the workload (full x and z
+    extent, `rows` updated rows through the cube's centre) with its medium
+    precomputed like the reference (src/precomp.c:85-105).  A y-slab keeps
+    the reference's OpenMP loop, which is parallel over z
+    (src/openmp_propagate.c:14-16), as parallel as on the whole cube."""
     from dc_gb300 import medium
     sx, sy, sz = geom.sizes
-    z0 = 4 + geom.absorb + SRC_DEPTH - planes // 2 - 4
-    spec = medium.with_origin(make_spec(geom), (0, 0, z0))
-    sizes = (sx, sy, planes + 8)
+    y0 = sy // 2 - rows // 2 - 4
+    spec = medium.with_origin(make_spec(geom), (0, y0, 0))
+    sizes = (sx, rows + 8, sz)
     aniso = medium.layered_fields(spec, sizes)
     coef = port.precomp(aniso)
     rng = np.random.Generator(np.random.PCG64(1))
-    shape = (sizes[2], sy, sx)
+    shape = (sz, sizes[1], sx)
     fields = [(rng.standard_normal(shape) * 1e-3).astype(np.float32) for _ in range(4)]
     return sizes, coef, fields
 
 
 def time_cpu_oracle(port, sizes, coef, fields, target_s: float, nthreads: int):
-    """Repeated oracle steps over the slab until ~target_s; returns
-    (updates/s, steps, seconds)."""
+    """Repeated oracle-port steps over the slab until ~target_s; returns
+    (updates/s, steps, seconds).  Used only where the reference's sources
+    are absent."""
     from oracle.oracle import KIND_F32
     sx, sy, sz = sizes
     pc, qc, pp, qp = fields
@@ -297,47 +308,79 @@ def time_cpu_oracle(port, sizes, coef, fields, target_s: float, nthreads: int):
     return pts * reps / el, reps, el
 
 
+def cpu_reference():
+    """The reference's own OpenMP path built with its own flags
+    (oracle/_ref/librefomp.so: src/openmp_propagate.c, -O3 -fopenmp), or
+    None where its sources are absent."""
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    from oracle.oracle import Reference
+    try:
+        return Reference("native")
+    except FileNotFoundError:
+        return None
+
+
+def cpu_baseline_slab(dc, geom, steps=None, target_s=12.0, warmup=1):
+    """CPU baseline on a y-slab of the workload (SLAB_ROWS updated rows, full
+    x and z extent): the reference's own OpenMP path through its one-rank
+    loop (kind "reference"), or the oracle port where the reference's
+    sources are absent (kind "port").  `steps` timed steps, or as many as
+    fill ~target_s.  Returns (updates/s, info dict)."""
+    from oracle.oracle import Port
+    port = Port()
+    ssizes, coef, fields = slab_inputs(dc, port, geom, SLAB_ROWS)
+    sx, sy, sz = ssizes
+    pts = (sx - 8) * (sy - 8) * (sz - 8)
+    ref = cpu_reference()
+    if ref is None:
+        nthreads = os.cpu_count() or 1
+        rate, reps, el = time_cpu_oracle(port, ssizes, coef, fields, target_s, nthreads)
+        return rate, {"kind": "port", "cores": nthreads, "steps": reps, "seconds": el,
+                      "what": "oracle port of src/openmp_propagate.c"}
+    shape = fields[0].shape
+    if warmup:
+        z = [np.zeros(shape, np.float32) for _ in range(4)]
+        ref.run(0, ssizes, (DX,) * 3, DT, warmup, *z, coef=coef)
+    if steps is None:
+        z = [np.zeros(shape, np.float32) for _ in range(4)]
+        _, _, one = ref.run(0, ssizes, (DX,) * 3, DT, 1, *z, coef=coef, timed=True)
+        steps = max(1, int(target_s / max(one, 1e-6)))
+    z = list(fields)
+    _, _, el = ref.run(0, ssizes, (DX,) * 3, DT, steps, *z, coef=coef, timed=True)
+    return pts * steps / el, {"kind": "reference", "cores": ref.threads(), "steps": steps,
+                              "seconds": el,
+                              "what": "the reference's src/openmp_propagate.c built with its "
+                                      "own flags (-O3 -fopenmp), its one-rank loop"}
+
+
 # ---------------------------------------------------------------------------
 def run_reference(args, rank, world):
-    """Reference arm: the CPU implementation of the path on the host cores."""
+    """Reference arm: the reference's own CPU implementation of the path on
+    the host cores (its OpenMP backend, built from its sources with its own
+    flags), one time step of a y-slab of the workload per timed step."""
     if rank != 0:
         return
-    from oracle import build_oracle
-    from oracle.oracle import KIND_F32, Port
     import __graft_entry__ as ge
     dc = ge.package()
     geom = geometry(args.n)
-    port = Port()
-    nthreads = os.cpu_count() or 1
-    kind = "port"
-    sizes, coef, fields = slab_inputs(dc, port, geom, SLAB_PLANES)
-    sx, sy, sz = sizes
-    pc, qc, pp, qp = fields
-    b0, b1 = (4, 4, 4), (sx - 4, sy - 4, sz - 4)
-    pts = (sx - 8) * (sy - 8) * (sz - 8)
-    for _ in range(args.warmup):
-        port.step(KIND_F32, sizes, b0, b1, (DX,) * 3, DT, pc, qc, pp, qp, coef=coef,
-                  nthreads=nthreads)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        port.step(KIND_F32, sizes, b0, b1, (DX,) * 3, DT, pc, qc, pp, qp, coef=coef,
-                  nthreads=nthreads)
-        pp, pc = pc, pp
-        qp, qc = qc, qp
-    el = time.perf_counter() - t0
-    value = pts * args.steps / el / 1e9
-    sample = (f"{args.steps} steps of the {sx - 8}x{sy - 8}x{sz - 8} updated slab "
-              f"(full x-y extent of the {geom.sizes[0]}^3 cube around the source depth)")
+    rate, info = cpu_baseline_slab(dc, geom, steps=args.steps, warmup=args.warmup)
+    value = rate / 1e9
+    sx, sz = geom.sizes[0] - 8, geom.sizes[2] - 8
+    sample = (f"{info['steps']} steps of the {sx}x{SLAB_ROWS}x{sz} updated slab (full x and z "
+              f"extent of the {geom.sizes[0]}^3 cube, {SLAB_ROWS} rows through its centre), "
+              f"{info['seconds']:.1f} s; {info['what']}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": info["seconds"] / info["steps"] * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded layered medium, numpy PCG64 seed 2026)",
         "config": {"workload": f"plain FP32 TTI, {args.n}^3 interior + {ABSORB} absorbing, "
-                               f"slab sample of {SLAB_PLANES} planes", "global_batch": 1,
-                   "seq_len": None, "parallelism": "cpu", "threads": nthreads},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind,
-                         "sample": sample},
+                               f"y-slab sample of {SLAB_ROWS} rows", "global_batch": 1,
+                   "seq_len": None, "parallelism": "cpu", "threads": info["cores"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"],
+                         "kind": info["kind"], "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -412,17 +455,14 @@ def run_ours(args, rank, world, local):
     if not args.no_e2e:
         e2e = run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_ms, world)
 
-    # ---- CPU baseline: the oracle on a slab (rank 0, N = 1) ---------------
+    # ---- CPU baseline: the reference's OpenMP path on a slab (rank 0, N = 1)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        from oracle.oracle import Port
-        port = Port()
-        nthreads = os.cpu_count() or 1
-        ssizes, coef, fields = slab_inputs(dc, port, geom, SLAB_PLANES)
-        rate, reps, el = time_cpu_oracle(port, ssizes, coef, fields, 12.0, nthreads)
-        cpu = {"value": rate / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
-               "sample": f"{reps} oracle steps of a {ssizes[0] - 8}x{ssizes[1] - 8}x"
-                         f"{ssizes[2] - 8} slab of the same workload ({el:.1f} s)"}
+        rate, info = cpu_baseline_slab(dc, geom)
+        cpu = {"value": rate / 1e9, "unit": UNIT, "cores": info["cores"], "kind": info["kind"],
+               "sample": f"{info['steps']} steps of a {geom.sizes[0] - 8}x{SLAB_ROWS}x"
+                         f"{geom.sizes[2] - 8} y-slab of the same workload "
+                         f"({info['seconds']:.1f} s); {info['what']}"}
 
     if rank != 0:
         return
@@ -605,15 +645,13 @@ def run_batched(args, rank, world, local):
     peak, peak_kind = peaks()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        from oracle.oracle import Port
-        port = Port()
-        nthreads = os.cpu_count() or 1
-        ssizes, coef, fields = slab_inputs(dc, port, geometry(N_INTERIOR), SLAB_PLANES)
-        rate, reps, el = time_cpu_oracle(port, ssizes, coef, fields, 12.0, nthreads)
-        cpu = {"value": rate / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
-               "sample": f"{reps} oracle steps of a {ssizes[0] - 8}x{ssizes[1] - 8}x"
-                         f"{ssizes[2] - 8} slab of the plain workload ({el:.1f} s); the "
-                         "per-update CPU cost does not depend on the batching"}
+        g2 = geometry(N_INTERIOR)
+        rate, info = cpu_baseline_slab(dc, g2)
+        cpu = {"value": rate / 1e9, "unit": UNIT, "cores": info["cores"], "kind": info["kind"],
+               "sample": f"{info['steps']} steps of a {g2.sizes[0] - 8}x{SLAB_ROWS}x"
+                         f"{g2.sizes[2] - 8} y-slab of the plain workload ({info['seconds']:.1f} s; "
+                         f"{info['what']}); the per-update CPU cost does not depend on the "
+                         "batching"}
     if rank != 0:
         return
     line = {
@@ -839,6 +877,141 @@ def run_best(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def run_refcuda(args, rank, world, local):
+    """The reference's own GPU path against ours on the same GPU and the
+    same inputs: the reference's default medium with its random velocity
+    boundary (vpz/vsv, constant angles: the only medium its CUDA backend
+    reads) on the plain workload's geometry, the reference's source at the
+    cube centre.  The reference runs its one-rank loop (seven dc_propagate
+    launches per step, each synchronised, src/worker.c:321-402 and
+    src/cuda_propagate.cu:32-69); ours runs the same steps as graph-replayed
+    single launches of the fast kernel on the (vpz, vsv) medium (32 B per
+    point-update), and once more through our library's reference ABI with
+    the same seven-box loop.  Both runs start from zero fields, so their
+    final fields are compared."""
+    import torch
+    import __graft_entry__ as ge
+    from oracle.oracle import Geometry, Reference, rel_l2
+    if rank != 0:
+        return
+    dc = ge.package()
+    dc.build()
+    torch.cuda.set_device(local)
+    ref = Reference("cuda")
+    geom = Geometry((args.n,) * 3, ABSORB)
+    sizes = geom.sizes
+    sx, sy, sz = sizes
+    dt = 1e-3
+    aniso = ref.default_anisotropy(geom.shape)
+    ref.random_velocity_boundary(sizes, sizes, (0, 0, 0), geom.n, 4, ABSORB,
+                                 aniso["vpz"], aniso["vsv"], 0)
+    vpz, vsv = aniso["vpz"], aniso["vsv"]
+    del aniso
+    steps = args.steps
+    src = np.array([ref.source(dt, it) for it in range(steps + args.warmup + 1)], np.float32)
+    pts = geom.compute_points
+    # the reference's CUDA path (its dc_device_data_init copies the host
+    # arrays; the loop time excludes set-up and the read-back)
+    z = [np.zeros(geom.shape, np.float32) for _ in range(4)]
+    ref.run(0, sizes, (DX,) * 3, dt, args.warmup, *z, vpz=vpz, vsv=vsv,
+            src_index=geom.source_index, src=src)
+    z = [np.zeros(geom.shape, np.float32) for _ in range(4)]
+    rpc, rqc, ref_s = ref.run(0, sizes, (DX,) * 3, dt, steps, *z, vpz=vpz, vsv=vsv,
+                              src_index=geom.source_index, src=src, timed=True)
+    del z
+    # ours: graph-replayed fast kernel on the vpz/vsv medium
+    sim = dc.Simulation(sizes, (DX,) * 3, dt, kernel=dc.KERNEL_FAST,
+                        medium=dc.MEDIUM_VPZ_VSV, device=local)
+    sim.set_vpz_vsv(vpz, vsv)
+    sim.set_fields()
+    sim.set_source(geom.source_index, src)
+    sim.run(args.warmup)
+    sim.set_fields()
+    sim.synchronize()
+    stream = torch.cuda.ExternalStream(sim.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        sim.run(steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    sim.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    f = sim.get_fields()
+    sim.close()
+    err = max(rel_l2(f["pc"], rpc), rel_l2(f["qc"], rqc))
+    # ours through the reference ABI, same seven-box loop
+    os.environ["DC_GB300_KERNEL"] = "fast"
+    os.environ["DC_GB300_MEDIUM"] = "vpz_vsv"
+    os.environ["DC_GB300_DEVICE"] = str(local)
+    proc = dc.Process(sizes, (DX,) * 3, dt, anisotropy={"vpz": vpz, "vsv": vsv},
+                      source_index=geom.source_index)
+    data = dc.device_data_init(proc)
+    r = 4
+    boxes = []
+    for side in range(2):
+        boxes.append(((r if side == 0 else sx - 2 * r, r, r),
+                      (2 * r if side == 0 else sx - r, sy - r, sz - r)))
+    for side in range(2):
+        boxes.append(((2 * r, r if side == 0 else sy - 2 * r, r),
+                      (sx - 2 * r, 2 * r if side == 0 else sy - r, sz - r)))
+    for side in range(2):
+        boxes.append(((2 * r, 2 * r, r if side == 0 else sz - 2 * r),
+                      (sx - 2 * r, sy - 2 * r, 2 * r if side == 0 else sz - r)))
+    boxes.append(((2 * r,) * 3, (sx - 2 * r, sy - 2 * r, sz - 2 * r)))
+    for it in range(args.warmup):
+        dc.device_add_source(data, geom.source_index, float(src[it]))
+        for b0, b1 in boxes:
+            dc.propagate(b0, b1, sizes, data, DX, DX, DX, dt)
+        dc.device_swap_arrays(data)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for it in range(steps):
+        dc.device_add_source(data, geom.source_index, float(src[it]))
+        for b0, b1 in boxes:
+            dc.propagate(b0, b1, sizes, data, DX, DX, DX, dt)
+        dc.device_swap_arrays(data)
+    dc.device_data_get_results(proc, data)
+    abi_s = time.perf_counter() - t0
+    dc.device_data_free(data)
+    for k in ("DC_GB300_KERNEL", "DC_GB300_MEDIUM", "DC_GB300_DEVICE"):
+        os.environ.pop(k, None)
+    ours = pts * steps / (ms * 1e-3) / 1e9
+    ref_rate = pts * steps / ref_s / 1e9
+    abi_rate = pts * steps / abi_s / 1e9
+    peak, peak_kind = peaks()
+    achieved = 32 * pts / (ms / steps * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": ours, "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (the reference's default medium + random velocity boundary, seed 0)",
+        "config": {"workload": f"reference CUDA path vs ours on one GB300: {args.n}^3 interior + "
+                               f"{ABSORB}-cell random velocity boundary, {sx}^3 padded, "
+                               "vpz/vsv medium (constant angles), FCUT 40 source at the centre, "
+                               "dt 1 ms",
+                   "form": "refcuda", "points_per_step": pts,
+                   "reference_cuda": {"gupd_s": ref_rate, "ms_per_step": ref_s / steps * 1e3,
+                                      "launches_per_step": 8,
+                                      "what": "src/cuda_propagate.cu + src/device_data.cu, nvcc "
+                                              "sm_103a, one-rank loop of src/worker.c"},
+                   "ours_graph": {"gupd_s": ours, "ms_per_step": ms / steps},
+                   "ours_reference_abi": {"gupd_s": abi_rate,
+                                          "ms_per_step": abi_s / steps * 1e3,
+                                          "note": "same seven-box loop through our dc_propagate, "
+                                                  "wall clock incl. the final read-back"},
+                   "speedup_vs_reference_cuda": ours / ref_rate,
+                   "rel_l2_vs_reference_cuda": err,
+                   "l2": "inputs 5.6 GB >> 129 MB L2; no flush"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "bytes_per_update": 32,
+                     "traffic": None},
+        "cpu_baseline": None, "e2e": None, "gpu_launches": steps, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -852,6 +1025,8 @@ def main():
             run_learned(args, rank, world, local)
         elif args.form == "best":
             run_best(args, rank, world, local)
+        elif args.form == "refcuda":
+            run_refcuda(args, rank, world, local)
         else:
             run_ours(args, rank, world, local)
     finally:

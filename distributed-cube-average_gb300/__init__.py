@@ -306,7 +306,10 @@ class Process:
             self._keep[name] = a
             setattr(p, name, fptr(a))
         if anisotropy is not None:
+            # names left out stay NULL (the vpz/vsv medium reads only those two)
             for n in ANISO_NAMES:
+                if anisotropy.get(n) is None:
+                    continue
                 a = _f32(anisotropy[n]).reshape(shape)
                 self._keep["a_" + n] = a
                 setattr(p.anisotropy_vars, n, fptr(a))

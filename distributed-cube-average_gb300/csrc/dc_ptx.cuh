@@ -70,7 +70,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
   }
 }
 
-// 3-D / 4-D tiled TMA loads global -> shared, completing on `bar`.
+// 3-D tiled TMA load global -> shared, completing on `bar`.
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map,
                                             int x, int y, int z,
                                             uint64_t *bar) {
@@ -78,17 +78,6 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map,
       "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::"
       "bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z),
-      "r"(smem_u32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map,
-                                            int x, int y, int z, int w,
-                                            uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::"
-      "bytes [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w),
       "r"(smem_u32(bar))
       : "memory");
 }

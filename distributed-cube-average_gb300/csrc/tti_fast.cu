@@ -303,21 +303,15 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
     mbar_arrive_expect_tx(&bars[s], Lay::TX_HALO + (want_lead ? Lay::TX_LEAD : 0u) +
                                         (want_out ? Lay::TX_OUT : 0u));
     tma_load_3d(st + Lay::OFF_H, tm_cur, x0 - kHalo, y0 - kHalo, k, &bars[s]);
-    // 16-byte groups are 4-D boxes (4 x 4-byte lanes innermost), 8- and
-    // 4-byte groups 3-D boxes of one element per point
-    if (want_lead) {
-      if (CB::L == 16)
-        tma_load_4d(st + Lay::OFF_L, tm_l, 0, mx0, my0, k + prm.moz, &bars[s]);
-      else
-        tma_load_3d(st + Lay::OFF_L, tm_l, mx0, my0, k + prm.moz, &bars[s]);
-    }
+    // 16-byte groups are mapped as two 8-byte elements per point (x
+    // coordinate 2 * x: one 512-byte row per tile row), 8- and 4-byte groups
+    // as one element per point
+    constexpr int XL = CB::L == 16 ? 2 : 1, XO = CB::O1 == 16 ? 2 : 1;
+    if (want_lead) tma_load_3d(st + Lay::OFF_L, tm_l, XL * mx0, my0, k + prm.moz, &bars[s]);
     if (want_out) {
       const int z = k - kHalo;
       const int mz = z + prm.moz;
-      if (CB::O1 == 16)
-        tma_load_4d(st + Lay::OFF_O1, tm_o1, 0, mx0, my0, mz, &bars[s]);
-      else
-        tma_load_3d(st + Lay::OFF_O1, tm_o1, mx0, my0, mz, &bars[s]);
+      tma_load_3d(st + Lay::OFF_O1, tm_o1, XO * mx0, my0, mz, &bars[s]);
       if (CB::O2) tma_load_3d(st + Lay::OFF_O2, tm_o2, mx0, my0, mz, &bars[s]);
       tma_load_3d(st + Lay::OFF_OWN, tm_prev, x0, y0, z, &bars[s]);
     }
@@ -692,19 +686,20 @@ bool fast_encode_medium_maps(int form, const float *coef, const void *coef16, co
   const uint64_t str8[2] = {P * 8, PL * 8};
   const uint64_t str4[2] = {P * 4, PL * 4};
   const uint32_t box_tile[3] = {kTX, static_cast<uint32_t>(ty), 1};
-  // 16-byte coefficient groups: 4 lanes of 4 bytes innermost
-  const uint64_t dims4[4] = {4, X, Y, Z};
-  const uint64_t str16[3] = {16, P * 16, PL * 16};
-  const uint32_t box16[4] = {4, kTX, static_cast<uint32_t>(ty), 1};
+  // 16-byte coefficient groups: two 8-byte elements per point, so a tile
+  // row is one 512-byte box row (a box whose innermost extent is a single
+  // 16-byte group makes the copy engine walk 32 x TY rows of 16 bytes)
+  const uint64_t dims16[3] = {2 * X, Y, Z};
+  const uint64_t str16[2] = {P * 16, PL * 16};
+  const uint32_t box16[3] = {2 * kTX, static_cast<uint32_t>(ty), 1};
   const auto U64 = CU_TENSOR_MAP_DATA_TYPE_UINT64, U32 = CU_TENSOR_MAP_DATA_TYPE_UINT32;
-  const auto F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
   const long long cnt = count;
   // out[0] = L (cxx, cyy, cxy, czz), out[1] = O1, out[2] = O2
   switch (form) {
     case CF_F32: {
       const char *c = reinterpret_cast<const char *>(coef);
-      return encode_tiled(&out[0], c, 4, dims4, str16, box16, err, F32) &&
-             encode_tiled(&out[1], c + cnt * 16, 4, dims4, str16, box16, err, F32) &&
+      return encode_tiled(&out[0], c, 3, dims16, str16, box16, err, U64) &&
+             encode_tiled(&out[1], c + cnt * 16, 3, dims16, str16, box16, err, U64) &&
              encode_tiled(&out[2], c + cnt * 32, 3, dims3, str8, box_tile, err, U64);
     }
     case CF_VV:

@@ -38,7 +38,9 @@ enum {
 enum {
   O_KIND_F32 = 0,        /* sample_compute (10 coefficient arrays), float */
   O_KIND_F32_REFCUDA = 1,/* sample_compute_optimized (vpz/vsv, const angles) */
-  O_KIND_F64 = 2         /* sample_compute restated in double precision */
+  O_KIND_F64 = 2,        /* sample_compute restated in double precision */
+  O_KIND_F64_SEP = 3     /* the same in double, cross terms as D_a(D_b p)
+                            (o_run only: whole compute region, 10 arrays) */
 };
 
 /* ---- medium set-up (host) ------------------------------------------- */
@@ -82,6 +84,13 @@ int o_step(int kind, long sx, long sy, long sz, const long b0[3],
            const void *pc, const void *qc, void *pp, void *qp,
            const float *const coef[O_NCOEF], const float *vpz,
            const float *vsv, const float *const sponge[3], int nthreads);
+
+/* One FP64 step over the whole compute region [4, s-4)^3 with the cross
+ * derivatives as D_a(D_b p) (see O_KIND_F64_SEP); work: 4 n doubles. */
+int o_step_f64_sep(long sx, long sy, long sz, float dx, float dy, float dz, float dt,
+                   const double *pc, const double *qc, double *pp, double *qp,
+                   const float *const coef[O_NCOEF], const float *const sponge[3],
+                   double *work, int nthreads);
 
 /* ---- time loop -------------------------------------------------------- */
 

@@ -1,8 +1,8 @@
 """ctypes bindings for the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
 ``Port`` wraps our C restatement (oracle/dc_oracle.c); ``Reference`` wraps
-the reference's own sources compiled into oracle/_ref/libref.so (present
-only where the reference checkout exists).  Only tests/, the smoke check and
+the reference's own sources compiled into oracle/_ref/ (present only where
+the reference checkout or its staged copy exists).  Only tests/, the smoke check and
 bench.py's CPU-baseline leg import this module -- it is the checker, never
 the product.
 
@@ -22,7 +22,7 @@ from . import build_oracle
 NCOEF = 10
 COEF_NAMES = ("ch1dxx", "ch1dyy", "ch1dzz", "ch1dxy", "ch1dyz", "ch1dxz",
               "v2px", "v2pz", "v2sz", "v2pn")
-KIND_F32, KIND_F32_REFCUDA, KIND_F64 = 0, 1, 2
+KIND_F32, KIND_F32_REFCUDA, KIND_F64, KIND_F64_SEP = 0, 1, 2, 3
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 
 _fp = C.POINTER(C.c_float)
@@ -155,7 +155,7 @@ class Port:
         """Time loop; field arrays are updated in place (copies are the
         caller's business).  Returns the final fields and optional
         traces [steps, nrec] and energy [steps]."""
-        dtype = np.float64 if kind == KIND_F64 else np.float32
+        dtype = np.float64 if kind in (KIND_F64, KIND_F64_SEP) else np.float32
         for a in (pp, pc, qp, qc):
             assert a.dtype == dtype and a.flags.c_contiguous
         cfg = _RunCfg()
@@ -197,21 +197,42 @@ class Port:
 
 
 class Reference:
-    """The reference's own sources (OpenMP backend + set-up), compiled from
-    the reference checkout.  Raises FileNotFoundError when unavailable."""
+    """The reference's own sources, compiled from the reference checkout or
+    its staged copy (oracle/build_oracle.py).  Raises FileNotFoundError when
+    unavailable.
 
-    def __init__(self):
-        so = build_oracle.build_ref()
+    variant "pin":    OpenMP backend, contraction off (bit-exact to the
+                      golden fixtures);
+    variant "native": OpenMP backend with the reference's own flags (the
+                      timed CPU baseline);
+    variant "cuda":   the reference's CUDA backend (needs a GPU to run).
+    """
+
+    BUILDERS = {"pin": "build_ref", "native": "build_ref_native", "cuda": "build_ref_cuda"}
+
+    def __init__(self, variant: str = "pin"):
+        so = getattr(build_oracle, self.BUILDERS[variant])()
         if so is None:
-            raise FileNotFoundError("reference checkout not present")
+            raise FileNotFoundError(f"reference build '{variant}' not available")
+        self.variant = variant
+        self.path = so
         lib = C.CDLL(str(so))
         lib.dc_calculate_source.argtypes = [C.c_float, C.c_int]
         lib.dc_calculate_source.restype = C.c_float
         lib.randomVelocityBoundaryPartition.argtypes = [C.c_int] * 14 + [_fp, _fp, C.POINTER(C.c_uint)]
-        lib.ref_run.argtypes = [C.c_int, C.c_long, C.c_long, C.c_long, C.c_float, C.c_float,
-                                C.c_float, C.c_float, C.c_int, C.c_long, _fp, C.POINTER(_fp),
-                                _fp, _fp, _fp, _fp, _fp, _fp, C.POINTER(_fp), C.POINTER(_fp)]
+        run_args = [C.c_int, C.c_long, C.c_long, C.c_long, C.c_float, C.c_float,
+                    C.c_float, C.c_float, C.c_int, C.c_long, _fp, C.POINTER(_fp),
+                    _fp, _fp, _fp, _fp, _fp, _fp, C.POINTER(_fp), C.POINTER(_fp)]
+        lib.ref_run.argtypes = run_args
+        lib.ref_run.restype = C.c_int
+        lib.ref_run_timed.argtypes = run_args + [_dp]
+        lib.ref_run_timed.restype = C.c_int
+        lib.ref_max_threads.restype = C.c_int
         self.lib = lib
+
+    def threads(self) -> int:
+        """OpenMP threads of the backend's parallel regions."""
+        return int(self.lib.ref_max_threads())
 
     def source(self, dt, it) -> float:
         return float(self.lib.dc_calculate_source(dt, it))
@@ -262,20 +283,27 @@ class Reference:
         return out
 
     def run(self, kind, sizes, d, dt, steps, pp, pc, qp, qc, coef=None, vpz=None, vsv=None,
-            src_index=-1, src=None):
-        """ref_run: the reference loop (OpenMP path, kind 0) or the reference
-        CUDA arithmetic on the host (kind 1).  Returns (pc, qc) copies of the
-        final fields."""
+            src_index=-1, src=None, timed=False):
+        """ref_run: the reference loop through the linked backend's
+        dc_propagate (kind 0: the OpenMP path with `coef`, or in the "cuda"
+        variant the reference's GPU path with vpz/vsv) or the reference CUDA
+        arithmetic replayed on the host (kind 1).  Returns (pc, qc) copies of
+        the final fields, and the time loop's wall seconds when `timed`."""
         sx, sy, sz = sizes
         cp = (_fp * NCOEF)(*[_f(c) for c in coef]) if coef is not None else None
         out_pc, out_qc = _fp(), _fp()
+        sec = C.c_double(0.0)
         src_arr = np.ascontiguousarray(src, np.float32) if src is not None else None
-        self.lib.ref_run(kind, sx, sy, sz, d[0], d[1], d[2], dt, steps, src_index, _f(src_arr),
-                         cp, _f(vpz), _f(vsv), _f(pp), _f(pc), _f(qp), _f(qc),
-                         C.byref(out_pc), C.byref(out_qc))
+        rc = self.lib.ref_run_timed(kind, sx, sy, sz, d[0], d[1], d[2], dt, steps, src_index,
+                                    _f(src_arr), cp, _f(vpz), _f(vsv), _f(pp), _f(pc), _f(qp),
+                                    _f(qc), C.byref(out_pc), C.byref(out_qc), C.byref(sec))
+        if rc != 0:
+            raise ValueError(f"kind {kind} is not available in the '{self.variant}' build")
         n = sx * sy * sz
         res_pc = np.ctypeslib.as_array(out_pc, (n,)).reshape(pc.shape).copy()
         res_qc = np.ctypeslib.as_array(out_qc, (n,)).reshape(qc.shape).copy()
+        if timed:
+            return res_pc, res_qc, sec.value
         return res_pc, res_qc
 
 
