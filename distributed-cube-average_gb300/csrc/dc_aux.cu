@@ -309,6 +309,24 @@ __global__ void coef_component_kernel(float *coef, float *dense, int k, long lon
   }
 }
 
+// Ten dense arrays in reference order (ch1dxx, ch1dyy, ch1dzz, ch1dxy,
+// ch1dyz, ch1dxz, v2px, v2pz, v2sz, v2pn) -> the three groups (cxx, cyy,
+// cxy, czz), (cxz, cyz, v2px, v2pz), (v2sz, v2pn) at the pitched index.
+// Reads are coalesced per array; one vector store per group.
+__global__ void coef_gather_kernel(float *coef, const CoefSources src, long long sx,
+                                   long long n, long long pitch, long long count) {
+  float4 *g0 = reinterpret_cast<float4 *>(coef);
+  float4 *g1 = reinterpret_cast<float4 *>(coef + 4 * count);
+  float2 *g2 = reinterpret_cast<float2 *>(coef + 8 * count);
+  for (long long d = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; d < n;
+       d += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long x = d % sx, i = (d / sx) * pitch + x;
+    g0[i] = make_float4(src.p[0][d], src.p[1][d], src.p[3][d], src.p[2][d]);
+    g1[i] = make_float4(src.p[5][d], src.p[4][d], src.p[6][d], src.p[7][d]);
+    g2[i] = make_float2(src.p[8][d], src.p[9][d]);
+  }
+}
+
 // max |v| over the four velocity terms, as float bits (non-negative floats
 // order like their bit patterns)
 __global__ void coef_vmax_kernel(const float *coef, long long count, unsigned int *out) {
@@ -377,6 +395,15 @@ cudaError_t launch_coef_vmax(cudaStream_t st, const float *coef, long long count
                              unsigned int *out) {
   const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((count + 255) / 256, 152 * 16)));
   coef_vmax_kernel<<<blocks, 256, 0, st>>>(coef, count, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coef_gather(cudaStream_t st, float *coef, const CoefSources &src,
+                               long long sx, long long sy, long long sz, long long pitch,
+                               long long count) {
+  const long long n = sx * sy * sz;
+  const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 32)));
+  coef_gather_kernel<<<blocks, 256, 0, st>>>(coef, src, sx, n, pitch, count);
   return cudaGetLastError();
 }
 

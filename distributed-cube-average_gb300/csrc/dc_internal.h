@@ -244,6 +244,16 @@ cudaError_t launch_precomp(cudaStream_t st, const float *theta,
 cudaError_t launch_coef_component(cudaStream_t st, float *coef, float *dense, int k,
                                   long long sx, long long sy, long long sz, long long pitch,
                                   long long count, bool to_grouped);
+// The ten dense coefficient arrays (dc_precomp_vars order, x fastest, no
+// pitch) -> grouped pitched coefficients in one pass; the sources may be any
+// memory the device can read (device, pinned host, or pageable host on
+// systems whose GPU uses the host page tables).
+struct CoefSources {
+  const float *p[10];
+};
+cudaError_t launch_coef_gather(cudaStream_t st, float *coef, const CoefSources &src,
+                               long long sx, long long sy, long long sz, long long pitch,
+                               long long count);
 // max |v2px|, |v2pz|, |v2sz|, |v2pn| as float bits, atomically into *out.
 cudaError_t launch_coef_vmax(cudaStream_t st, const float *coef, long long count,
                              unsigned int *out);

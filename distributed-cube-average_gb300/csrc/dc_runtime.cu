@@ -42,6 +42,45 @@ int fail(int code, const std::string &msg) {
 
 long long round_up4(long long v) { return (v + 3) / 4 * 4; }
 
+// The address at which kernels on `dev` may read or write the caller's array
+// `p` in place, or nullptr when it has to be staged through a copy.  Direct
+// access covers device memory of `dev`, managed memory, pinned or registered
+// host memory and -- where the GPU reaches pageable memory through the host's
+// page tables (NVLink-C2C systems such as GB300) -- plain malloc'd memory.
+// Reading in place moves the data once, at the link's bandwidth, with no
+// staging buffer.  DC_GB300_STAGED_COPIES=1 stages every host array.
+template <typename T>
+T *direct_view(T *p, int dev) {
+  if (!p) return nullptr;
+  static const bool staged = [] {
+    const char *e = std::getenv("DC_GB300_STAGED_COPIES");
+    return e && std::strcmp(e, "1") == 0;
+  }();
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  switch (a.type) {
+    case cudaMemoryTypeDevice:
+      return a.device == dev ? p : nullptr;
+    case cudaMemoryTypeManaged:
+      return p;
+    case cudaMemoryTypeHost:
+      return staged ? nullptr : static_cast<T *>(a.devicePointer);
+    default: {
+      if (staged) return nullptr;
+      int ats = 0;
+      if (cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) !=
+          cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+      }
+      return ats ? p : nullptr;
+    }
+  }
+}
+
 Sim *impl(dc_gb300_sim *h) { return h ? h->impl : nullptr; }
 
 // Pair buffer that holds the field whose p component is `p` and q component
@@ -497,6 +536,16 @@ extern "C" int dc_gb300_set_precomp(dc_gb300_sim *h, const dc_precomp_vars *host
     if (!p) return fail(DC_GB300_ERR_ARG, "a coefficient array is null");
   DCG_TRY(cudaSetDevice(s->device));
   const long long n = s->sx * s->sy * s->sz;
+  CoefSources views{};
+  bool direct = true;
+  for (int k = 0; k < 10; ++k) direct = direct && (views.p[k] = direct_view(src[k], s->device));
+  if (direct) {  // one pass, reading the caller's arrays in place
+    DCG_TRY(launch_coef_gather(s->stream, s->coef, views, s->sx, s->sy, s->sz, s->pitch,
+                               s->count));
+    DCG_TRY(cudaStreamSynchronize(s->stream));
+    s->coef16_stale = true;
+    return DC_GB300_OK;
+  }
   float *stage = nullptr;
   DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n, s->stream));
   for (int k = 0; k < 10; ++k) {
@@ -516,6 +565,13 @@ extern "C" int dc_gb300_set_vpz_vsv(dc_gb300_sim *h, const float *vpz, const flo
   if (!s->vv) return fail(DC_GB300_ERR_STATE, "simulation uses the ten-coefficient medium form");
   DCG_TRY(cudaSetDevice(s->device));
   const long long n = s->sx * s->sy * s->sz;
+  const float *dv = direct_view(vpz, s->device), *ds = direct_view(vsv, s->device);
+  if (dv && ds) {
+    DCG_TRY(launch_pack(s->stream, reinterpret_cast<float2 *>(s->vv), dv, ds, s->sx, s->sy,
+                        s->sz, s->pitch));
+    DCG_TRY(cudaStreamSynchronize(s->stream));
+    return DC_GB300_OK;
+  }
   float *stage = nullptr;
   DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
   DCG_TRY(cudaMemcpyAsync(stage, vpz, sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
@@ -569,10 +625,18 @@ extern "C" int dc_gb300_get_vpz_vsv(dc_gb300_sim *h, float *vpz, float *vsv) {
 namespace {
 // GPU FP64 precompute from dense host anisotropy arrays into `grouped`, a
 // dense grouped coefficient block of n points (coef_index with count = n).
-int precompute_dense(cudaStream_t st, const dc_anisotropy_t *a, long long n, float *grouped) {
+int precompute_dense(cudaStream_t st, int dev, const dc_anisotropy_t *a, long long n,
+                     float *grouped) {
   const float *src[6] = {a->theta, a->phi, a->vsv, a->vpz, a->epsilon, a->delta};
   for (const float *p : src)
     if (!p) return fail(DC_GB300_ERR_ARG, "an anisotropy array is null");
+  const float *v[6];
+  bool direct = true;
+  for (int k = 0; k < 6; ++k) direct = direct && (v[k] = direct_view(src[k], dev));
+  if (direct) {
+    DCG_TRY(launch_precomp(st, v[0], v[1], v[2], v[3], v[4], v[5], grouped, n, n));
+    return DC_GB300_OK;
+  }
   float *d_in = nullptr;
   DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&d_in), sizeof(float) * n * 6, st));
   for (int k = 0; k < 6; ++k)
@@ -628,7 +692,7 @@ extern "C" int dc_gb300_set_anisotropy(dc_gb300_sim *h, const dc_anisotropy_t *h
     float *grouped = nullptr;
     DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&grouped), sizeof(float) * n * DC_NCOEF,
                             s->stream));
-    int rc = precompute_dense(s->stream, host, n, grouped);
+    int rc = precompute_dense(s->stream, s->device, host, n, grouped);
     if (rc != DC_GB300_OK) return rc;
     DCG_TRY(launch_coef_repitch(s->stream, s->coef, grouped, s->sx, s->sy, s->sz, s->pitch,
                                 s->count));
@@ -685,11 +749,26 @@ extern "C" int dc_gb300_set_fields(dc_gb300_sim *h, const float *pp, const float
   int cur = -1, prev = -1;
   if (!roles(s, &cur, &prev)) return fail(DC_GB300_ERR_STATE, "field pointers rearranged");
   const long long n = s->sx * s->sy * s->sz;
-  float *stage = nullptr;
-  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
   const float *src[2][2] = {{pp, qp}, {pc, qc}};
   const int dst[2] = {prev, cur};
-  for (int k = 0; k < 2; ++k) {
+  bool direct = true;
+  const float *view[2][2];
+  for (int k = 0; k < 2; ++k)
+    for (int c = 0; c < 2; ++c) {
+      view[k][c] = direct_view(src[k][c], s->device);
+      direct = direct && (!src[k][c] || view[k][c]);
+    }
+  float *stage = nullptr;
+  if (direct) {  // pack straight from the caller's arrays
+    for (int k = 0; k < 2; ++k) {
+      DCG_TRY(cudaMemsetAsync(s->pq[dst[k]], 0, sizeof(float2) * s->count, s->stream));
+      DCG_TRY(launch_pack(s->stream, s->pq[dst[k]], view[k][0], view[k][1], s->sx, s->sy,
+                          s->sz, s->pitch));
+    }
+  } else {
+    DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
+  }
+  for (int k = 0; k < 2 && !direct; ++k) {
     const float *dp = nullptr, *dq = nullptr;
     if (src[k][0]) {
       DCG_TRY(cudaMemcpyAsync(stage, src[k][0], sizeof(float) * n, cudaMemcpyHostToDevice,
@@ -705,7 +784,7 @@ extern "C" int dc_gb300_set_fields(dc_gb300_sim *h, const float *pp, const float
     DCG_TRY(cudaMemsetAsync(s->pq[dst[k]], 0, sizeof(float2) * s->count, s->stream));
     DCG_TRY(launch_pack(s->stream, s->pq[dst[k]], dp, dq, s->sx, s->sy, s->sz, s->pitch));
   }
-  DCG_TRY(cudaFreeAsync(stage, s->stream));
+  if (stage) DCG_TRY(cudaFreeAsync(stage, s->stream));
   DCG_TRY(cudaMemsetAsync(s->d_step, 0, sizeof(int), s->stream));
   if (s->d_energy) DCG_TRY(cudaMemsetAsync(s->d_energy, 0, sizeof(double) * s->energy_cap, s->stream));
   if (s->d_traces)
@@ -724,11 +803,25 @@ extern "C" int dc_gb300_get_fields(dc_gb300_sim *h, float *pp, float *pc, float 
   int cur = -1, prev = -1;
   if (!roles(s, &cur, &prev)) return fail(DC_GB300_ERR_STATE, "field pointers rearranged");
   const long long n = s->sx * s->sy * s->sz;
-  float *stage = nullptr;
-  DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
   float *dst[2][2] = {{pp, qp}, {pc, qc}};
   const int src[2] = {prev, cur};
-  for (int k = 0; k < 2; ++k) {
+  bool direct = true;
+  float *view[2][2];
+  for (int k = 0; k < 2; ++k)
+    for (int c = 0; c < 2; ++c) {
+      view[k][c] = direct_view(dst[k][c], s->device);
+      direct = direct && (!dst[k][c] || view[k][c]);
+    }
+  float *stage = nullptr;
+  if (direct) {  // unpack straight into the caller's arrays
+    for (int k = 0; k < 2; ++k)
+      if (dst[k][0] || dst[k][1])
+        DCG_TRY(launch_unpack(s->stream, s->pq[src[k]], view[k][0], view[k][1], s->sx, s->sy,
+                              s->sz, s->pitch));
+  } else {
+    DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&stage), sizeof(float) * n * 2, s->stream));
+  }
+  for (int k = 0; k < 2 && !direct; ++k) {
     if (!dst[k][0] && !dst[k][1]) continue;
     DCG_TRY(launch_unpack(s->stream, s->pq[src[k]], stage, stage + n, s->sx, s->sy, s->sz,
                           s->pitch));
@@ -739,7 +832,7 @@ extern "C" int dc_gb300_get_fields(dc_gb300_sim *h, float *pp, float *pc, float 
       DCG_TRY(cudaMemcpyAsync(dst[k][1], stage + n, sizeof(float) * n, cudaMemcpyDeviceToHost,
                               s->stream));
   }
-  DCG_TRY(cudaFreeAsync(stage, s->stream));
+  if (stage) DCG_TRY(cudaFreeAsync(stage, s->stream));
   float pre[2] = {0.f, 0.f};
   const bool patch = source_pending(s) && (pc || qc);
   if (patch)
@@ -1493,7 +1586,9 @@ extern "C" dc_precomp_vars dc_compute_precomp_vars(int sx, int sy, int sz,
     set_error("CUDA set-up failed in dc_compute_precomp_vars");
     abi_die("dc_compute_precomp_vars");
   }
-  if (precompute_dense(st, &anisotropy, n, grouped) != DC_GB300_OK)
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      precompute_dense(st, dev, &anisotropy, n, grouped) != DC_GB300_OK)
     abi_die("dc_compute_precomp_vars");
   for (int k = 0; k < 10; ++k)
     if (launch_coef_component(st, grouped, stage, kRefOrder[k], sx, sy, sz, sx, n, false) !=

@@ -118,7 +118,12 @@ void dc_propagate(const size_t start_coords[3], const size_t end_coords[3],
  * Environment: DC_GB300_KERNEL=fast|exact selects the stencil arithmetic;
  * DC_GB300_MEDIUM=precomp|vpz_vsv selects the medium form (vpz_vsv = the
  * reference CUDA backend's constant-angle arithmetic,
- * include/sample_compute.h:9-18). */
+ * include/sample_compute.h:9-18).
+ * Host arrays the GPU can address (pinned or registered memory, and plain
+ * malloc'd memory where the GPU reads pageable memory through the host's
+ * page tables, as on NVLink-C2C systems) are read in place by the packing
+ * kernels, one pass at the link's bandwidth; other memory is staged through
+ * copies.  DC_GB300_STAGED_COPIES=1 stages every host array. */
 dc_device_data *dc_device_data_init(dc_process_t *process);
 
 /* include/device_data.h:19 -- src/device_data.cu:96-105 */
@@ -242,7 +247,8 @@ dc_device_data *dc_gb300_device_data(dc_gb300_sim *sim);
 dc_gb300_sim *dc_gb300_from_device_data(dc_device_data *data);
 long dc_gb300_device_pitch(const dc_gb300_sim *sim);
 
-/* Medium from dense host arrays (sx*sy*sz floats each). */
+/* Medium from dense host arrays (sx*sy*sz floats each; read in place when
+ * the GPU can address them, see dc_device_data_init). */
 int dc_gb300_set_precomp(dc_gb300_sim *sim, const dc_precomp_vars *host);
 int dc_gb300_set_vpz_vsv(dc_gb300_sim *sim, const float *vpz,
                          const float *vsv);
@@ -292,7 +298,8 @@ int dc_gb300_generate_layered(dc_gb300_sim *sim,
  * counter to 0. */
 int dc_gb300_set_fields(dc_gb300_sim *sim, const float *pp, const float *pc,
                         const float *qp, const float *qc);
-/* Copies the fields to dense host arrays (NULL skips one).  Synchronous. */
+/* Copies the fields to dense host arrays (NULL skips one; written in place
+ * when the GPU can address them).  Synchronous. */
 int dc_gb300_get_fields(dc_gb300_sim *sim, float *pp, float *pc, float *qp,
                         float *qc);
 

@@ -377,16 +377,11 @@ int o_step_f64_sep(long sx, long sy, long sz, float dx, float dy, float dz, floa
   a.dt2 = (double)dt * (double)dt;
   a.sY = sx;
   a.sZ = sx * sy;
-  /* planes in order, rows of a plane across the threads: the nine planes
-   * the z-derivatives read are shared by all threads and stay in cache */
-#pragma omp parallel num_threads(nthreads)
-  for (long z = 4; z < sz - 4; ++z) {
-#pragma omp for schedule(static)
-    for (long y = 4; y < sy - 4; ++y) {
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+  for (long z = 4; z < sz - 4; ++z)
+    for (long y = 4; y < sy - 4; ++y)
       sep_row(&a, y * a.sY + z * a.sZ, 4, sx - 4, pc, qc, pp, qp, pxd, pyd, qxd, qyd, gxa,
               gya[y], gza[z]);
-    }
-  }
   free(ones);
   return 0;
 }
