@@ -129,6 +129,8 @@ def parse():
                     help="learned form: interior cells per axis")
     ap.add_argument("--no-judge", action="store_true",
                     help="learned form: skip the reflected-energy judge")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="mixed/batched/best forms: skip the FP64-oracle accuracy check")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"batched": 1000, "learned": 1500, "best": 1000,
@@ -355,6 +357,107 @@ def cpu_baseline_slab(dc, geom, steps=None, target_s=12.0, warmup=1):
 
 
 # ---------------------------------------------------------------------------
+# Accuracy against the FP64 CPU oracle (outside every timed region)
+ACC_CROP_N = 160      # the mixed form's check: 160^3 interior + 48-cell sponge = 256^3 updated
+
+
+def receiver_grid(sizes, pad: int, n_xy, nx: int = 32, ny: int = 16, depth: int = 8):
+    """nx x ny receivers spread over the interior's x-y extent at interior
+    depth `depth` (global z = pad + depth); linear indices."""
+    sx, sy, _ = sizes
+    xs = np.linspace(pad, pad + n_xy[0] - 1, nx).round().astype(np.int64)
+    ys = np.linspace(pad, pad + n_xy[1] - 1, ny).round().astype(np.int64)
+    z = pad + depth
+    return np.array([x + y * sx + z * sx * sy for y in ys for x in xs], np.int64)
+
+
+def oracle_f64(sizes, coef, steps, src_idx, src, sponge, rec):
+    """The FP64 CPU oracle (oracle/dc_oracle.c, double precision, cross
+    terms in separable form) over `steps` steps from zero fields."""
+    from oracle.oracle import KIND_F64_SEP, Port
+    port = Port()
+    shape = (sizes[2], sizes[1], sizes[0])
+    z = [np.zeros(shape, np.float64) for _ in range(4)]
+    t0 = time.perf_counter()
+    r = port.run(KIND_F64_SEP, sizes, (DX,) * 3, DT, steps, *z, coef=coef, src_index=src_idx,
+                 src=src, sponge=sponge, rec=rec)
+    return r, time.perf_counter() - t0
+
+
+def rel(a, b) -> float:
+    from oracle.oracle import rel_l2
+    return rel_l2(a, b)
+
+
+def gpu_box_run(dc, sizes, spec, form, steps, src_idx, src, sponge, rec, local):
+    """One GPU run of a box of the seeded medium with the given coefficient
+    storage; returns (pc, qc, traces, FP32 coefficients)."""
+    sim = dc.Simulation(sizes, (DX,) * 3, DT, kernel=dc.KERNEL_FAST, medium=form, device=local)
+    sim.generate_layered(spec)
+    sim.set_fields()
+    sim.set_source(src_idx, src)
+    if sponge is not None:
+        sim.set_sponge(*sponge)
+    sim.set_receivers(rec, steps)
+    sim.run(steps)
+    sim.synchronize()
+    f = sim.get_fields()
+    tr = sim.traces(steps)
+    coef = sim.get_precomp()
+    sim.close()
+    return f["pc"], f["qc"], tr, coef
+
+
+def mixed_accuracy(dc, big_geom, form, storage: str, steps: int, local: int):
+    """The mixed form's error on its own workload: a 256^3 crop of the
+    1024 x 1024 x 768 run (160^3 interior + the 48-cell sponge, the same
+    medium origin, source depth and number of steps, centred on the source
+    horizontally) run as its own box in the narrow storage and in FP32,
+    both against the FP64 CPU oracle on the same box; wavefield and a
+    32 x 16 = 512-receiver grid at interior depth 8."""
+    from dc_gb300 import medium
+    crop = geometry(ACC_CROP_N)
+    sizes = crop.sizes
+    bsx, bsy, _ = big_geom.sizes
+    origin = (bsx // 2 - sizes[0] // 2, bsy // 2 - sizes[1] // 2, 0)
+    spec = medium.with_origin(make_spec(big_geom), origin)
+    o = 4 + ABSORB
+    src_idx = crop.index(sizes[0] // 2, sizes[1] // 2, o + SRC_DEPTH)
+    src = dc.source_table(DT, steps + 1, FCUT)
+    sponge = [dc.sponge_profile(v, ABSORB, SPONGE_KAPPA) for v in sizes]
+    rec = receiver_grid(sizes, o, crop.n[:2])
+    pc, qc, tr, coef = gpu_box_run(dc, sizes, spec, form, steps, src_idx, src, sponge, rec, local)
+    pc32, qc32, tr32, _ = gpu_box_run(dc, sizes, spec, dc.MEDIUM_PRECOMP, steps, src_idx, src,
+                                      sponge, rec, local)
+    f64, osec = oracle_f64(sizes, coef, steps, src_idx, src, sponge, rec)
+    return {"check": f"FP64 CPU oracle on a {sizes[0] - 8}^3 crop ({ACC_CROP_N}^3 interior + "
+                     f"{ABSORB}-cell sponge) of the same run, origin {origin}, {steps} steps, "
+                     f"{rec.size} receivers", "storage": storage,
+            "rel_l2_p": rel(pc, f64.pc), "rel_l2_q": rel(qc, f64.qc),
+            "rel_l2_traces": rel(tr, f64.traces),
+            "fp32_rel_l2_p": rel(pc32, f64.pc), "fp32_rel_l2_traces": rel(tr32, f64.traces),
+            "bar": 1e-3, "meets_bar": bool(rel(pc, f64.pc) <= 1e-3 and rel(tr, f64.traces) <= 1e-3),
+            "oracle_seconds": osec}
+
+
+def shot_coef(dc, spec_box, shot, local):
+    """FP32 coefficients of a shot's crop of the shared medium (the values
+    the batch reads at the crop: the medium is evaluated per point at global
+    coordinates)."""
+    from dc_gb300 import medium
+    sim = dc.Simulation(shot["sizes"], (DX,) * 3, DT, kernel=dc.KERNEL_FAST, device=local)
+    sim.generate_layered(medium.with_origin(spec_box, shot["origin"]))
+    coef = sim.get_precomp()
+    sim.close()
+    return coef
+
+
+def shot_index(sizes, xyz) -> int:
+    sx, sy, _ = sizes
+    return int(xyz[0] + xyz[1] * sx + xyz[2] * sx * sy)
+
+
+# ---------------------------------------------------------------------------
 def run_reference(args, rank, world):
     """Reference arm: the reference's own CPU implementation of the path on
     the host cores (its OpenMP backend, built from its sources with its own
@@ -450,6 +553,11 @@ def run_ours(args, rank, world, local):
                   else None)
     sim.close()
 
+    # ---- the mixed form's error against the FP64 CPU oracle ---------------
+    accuracy = None
+    if args.form == "mixed" and rank == 0 and not args.no_accuracy:
+        accuracy = mixed_accuracy(dc, geom, medium_form, args.medium, args.steps, local)
+
     # ---- end to end through the reference ABI with host buffers ----------
     e2e = None
     if not args.no_e2e:
@@ -477,13 +585,13 @@ def run_ours(args, rank, world, local):
                    if args.form == "plain" else
                    (f"mixed precision: {'x'.join(map(str, args.nxyz))} interior + "
                     f"{ABSORB}-cell sponge, {args.medium.upper()} medium storage, FP32 math "
-                    f"and wavefields, dt 0.8 ms, 20 Hz Ricker; rel. L2 vs FP64 oracle "
-                    f"stated by tests/test_gpu_mixed.py"),
+                    f"and wavefields, dt 0.8 ms, 20 Hz Ricker; rel. L2 vs the FP64 oracle "
+                    f"in config.accuracy"),
                    "form": args.form,
                    "kernel": args.kernel, "medium_storage": args.medium,
                    "points_per_step": pts, "global_batch": world,
                    "seq_len": None, "parallelism": f"shots{world}" if world > 1 else "single",
-                   "l2": "inputs 13 GB >> 129 MB L2; no flush"},
+                   "l2": "inputs 13 GB >> 129 MB L2; no flush", "accuracy": accuracy},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "bytes_per_update": bytes_per_update,
@@ -638,6 +746,28 @@ def run_batched(args, rank, world, local):
     ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
     tr = b.traces(0, total)
     assert np.isfinite(tr).all()
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        # the smallest shot, as the batch computed it, against the FP64 oracle
+        k = min(range(len(shots)), key=lambda i: int(np.prod(shots[i]["sizes"])))
+        sh = shots[k]
+        f = b.get_fields(k)
+        btr = b.traces(k, total)
+        coef = shot_coef(dc, medium.layered_spec(MEDIUM_SEED, mbox), sh, local)
+        sizes = sh["sizes"]
+        rec = np.array([shot_index(sizes, r) for r in sh["rec"]], np.int64)
+        f64, osec = oracle_f64(sizes, coef, total, shot_index(sizes, sh["src"]),
+                               dc.source_table(DT, total + 1, sh["fcut"]),
+                               [dc.sponge_profile(v, ABSORB, SPONGE_KAPPA) for v in sizes], rec)
+        accuracy = {"check": f"shot {k} of the batch (the smallest, {sizes[0]}x{sizes[1]}x"
+                             f"{sizes[2]} padded) after all {total} steps against the FP64 "
+                             f"CPU oracle on its crop; {rec.size} receivers",
+                    "storage": storage, "rel_l2_p": rel(f["pc"], f64.pc),
+                    "rel_l2_q": rel(f["qc"], f64.qc), "rel_l2_traces": rel(btr, f64.traces),
+                    "bar": 1e-3,
+                    "meets_bar": bool(rel(f["pc"], f64.pc) <= 1e-3 and
+                                      rel(btr, f64.traces) <= 1e-3),
+                    "oracle_seconds": osec}
     b.close()
     value = weak_rate(pts, args.steps, world, ms)
     bytes_per_update = 44 if storage in ("f16", "bf16") else 64
@@ -670,7 +800,7 @@ def run_batched(args, rank, world, local):
                                                      "autotune_ms_per_step": tune_ms},
                    "global_batch": args.shots * world, "seq_len": None,
                    "parallelism": f"shots{args.shots}x{world}",
-                   "l2": "inputs ~76 GB >> 129 MB L2; no flush"},
+                   "l2": "inputs ~76 GB >> 129 MB L2; no flush", "accuracy": accuracy},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "bytes_per_update": bytes_per_update, "traffic": None},
@@ -766,6 +896,56 @@ def run_learned(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def best_accuracy(dc, b, thin, wide, spec, total: int, layer: int, local: int):
+    """The best form's error on its own workload: the smallest shot, as the
+    batch computed it (FP16 medium, learned thin layer), against the FP64
+    CPU oracle of the same shot in the plain form's geometry (the 48-cell
+    sponge), compared over the shot's interior and its receivers; the plain
+    FP32 form of the same shot against the same oracle for comparison."""
+    k = min(range(len(thin)), key=lambda i: int(np.prod(wide[i]["sizes"])))
+    t, w = thin[k], wide[k]
+    pt, pw = layer + 4, BATCH_PAD
+    nx, ny = w["sizes"][0] - 2 * pw, w["sizes"][1] - 2 * pw
+    nz = w["sizes"][2] - 2 * pw
+
+    def inner(a, pad):
+        return a[pad:pad + nz, pad:pad + ny, pad:pad + nx]
+
+    f = b.get_fields(k)
+    btr = b.traces(k, total)
+    sizes = w["sizes"]
+    coef = shot_coef(dc, spec, w, local)
+    src_idx = shot_index(sizes, w["src"])
+    src = dc.source_table(DT, total + 1, w["fcut"])
+    sponge = [dc.sponge_profile(v, ABSORB, SPONGE_KAPPA) for v in sizes]
+    rec = np.array([shot_index(sizes, r) for r in w["rec"]], np.int64)
+    f64, osec = oracle_f64(sizes, coef, total, src_idx, src, sponge, rec)
+    # the plain form (FP32, 48-cell sponge) of the same shot on the GPU
+    sim = dc.Simulation(sizes, (DX,) * 3, DT, kernel=dc.KERNEL_FAST, device=local)
+    sim.set_precomp(coef)
+    sim.set_fields()
+    sim.set_source(src_idx, src)
+    sim.set_sponge(*sponge)
+    sim.set_receivers(rec, total)
+    sim.run(total)
+    sim.synchronize()
+    pf = sim.get_fields()
+    ptr = sim.traces(total)
+    sim.close()
+    e_p = rel(inner(f["pc"], pt), inner(f64.pc, pw))
+    e_tr = rel(btr, f64.traces)
+    return {"check": f"shot {k} of the batch (the smallest: {nx}x{ny}x{nz} interior) after "
+                     f"all {total} steps against the FP64 CPU oracle of the same shot with the "
+                     f"{ABSORB}-cell sponge, over the interior and {rec.size} receivers",
+            "rel_l2_p_interior": e_p, "rel_l2_q_interior": rel(inner(f["qc"], pt),
+                                                               inner(f64.qc, pw)),
+            "rel_l2_traces": e_tr,
+            "plain_fp32_rel_l2_p_interior": rel(inner(pf["pc"], pw), inner(f64.pc, pw)),
+            "plain_fp32_rel_l2_traces": rel(ptr, f64.traces),
+            "bar": 1e-3, "meets_bar": bool(e_p <= 1e-3 and e_tr <= 1e-3),
+            "oracle_seconds": osec}
+
+
 def run_best(args, rank, world, local):
     """Best form (batched + FP16 medium + learned thin layer) against the
     plain form on the same shot layout."""
@@ -814,6 +994,9 @@ def run_best(args, rank, world, local):
     launches = b.launches - l0
     assert np.isfinite(b.traces(0, total)).all()
     compute_pts = b.points
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        accuracy = best_accuracy(dc, b, thin, wide, spec, total, layer, local)
     b.close()
     mlp.close()
     best = interior * args.steps / (ms * 1e-3) / 1e9
@@ -860,10 +1043,7 @@ def run_best(args, rank, world, local):
                              "steps_per_shot": plain_steps,
                              "ms_per_step_all_shots": plain_ms / plain_steps},
                    "speedup_vs_plain": best / plain,
-                   "accuracy": "FP16 medium: rel. L2 vs FP64 oracle 3.2e-4 (batched shot, 70 "
-                               "steps) and 7.3e-4 (300 steps); learned layer: reflected energy "
-                               "0.060 vs 0.0013 for the 48-cell sponge (384^3, 32-cell band, "
-                               "1503 steps; bench.py --form learned)",
+                   "accuracy": accuracy,
                    "global_batch": args.shots * world, "seq_len": None,
                    "parallelism": f"shots{args.shots}x{world}",
                    "l2": "inputs ~40 GB >> 129 MB L2; no flush"},

@@ -613,7 +613,7 @@ extern "C" int dc_gb300_batch_create(const dc_gb300_batch_config *cfg, dc_gb300_
                  : cfg->medium == DC_GB300_MEDIUM_PRECOMP_BF16 ? dcg::CF_BF16
                                                                : dcg::CF_F32;
   b->max_steps = cfg->max_steps;
-  b->ty = dcg::fast_default_ty();
+  b->ty = dcg::fast_default_ty(b->coef_form);
   auto bail = [&](int code, const std::string &msg) {
     dcg::release(b);
     delete h;
@@ -854,8 +854,10 @@ extern "C" int dc_gb300_batch_set_learned_layer(dc_gb300_batch *h, const dc_gb30
 extern "C" int dc_gb300_batch_set_tiles(dc_gb300_batch *h, int ty, int zsplit) {
   Batch *b = dcg::impl(h);
   if (!b) return fail(DC_GB300_ERR_ARG, "null batch");
-  if ((ty != 8 && ty != 16) || zsplit < 1 || zsplit > 64)
-    return fail(DC_GB300_ERR_ARG, "tile rows must be 8 or 16 and zsplit in [1, 64]");
+  if (!dcg::fast_tile_rows_valid(ty, b->coef_form) || zsplit < 1 || zsplit > 64)
+    return fail(DC_GB300_ERR_ARG,
+                "tile rows must be 8 or 16 (or 6 with an FP16/BF16 medium) and zsplit in "
+                "[1, 64]");
   BATCH_TRY(cudaSetDevice(b->device));
   b->ty = ty;
   b->zsplit = zsplit;
@@ -870,7 +872,9 @@ extern "C" int dc_gb300_batch_autotune(dc_gb300_batch *h, int steps, int *ty_out
   if (!b) return fail(DC_GB300_ERR_ARG, "null batch");
   if (steps < 1) return fail(DC_GB300_ERR_ARG, "autotune needs at least one step");
   BATCH_TRY(cudaSetDevice(b->device));
-  const int tys[2] = {8, 16};
+  // tile rows 6 (three CTAs per SM) exist for the FP16/BF16 forms only
+  std::vector<int> tys = {8, 16};
+  if (dcg::fast_tile_rows_valid(6, b->coef_form)) tys.push_back(6);
   const int splits[4] = {1, 2, 4, 8};
   int best_ty = b->ty, best_split = b->zsplit;
   bool best_persistent = b->persistent;

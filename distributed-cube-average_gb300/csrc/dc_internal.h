@@ -189,9 +189,12 @@ struct FastShape {
 };
 FastShape fast_shape(const Sim *sim);
 bool fast_encode_maps(Sim *sim, std::string *err);
-// Tile rows (TY) of the single-simulation fast kernel (8 unless
-// DC_GB300_FAST_TY=16).
-int fast_default_ty();
+// Tile rows (TY) of the fast kernel for coefficient form `form`: 8 unless
+// DC_GB300_FAST_TY selects 16, or 6 (FP16/BF16 forms only).
+int fast_default_ty(int form);
+// Whether tile rows `ty` are compiled for coefficient form `form` (8 and 16
+// for every form, 6 for the FP16/BF16 forms).
+bool fast_tile_rows_valid(int ty, int form);
 // Tensor maps of one (p, q) pair buffer for tiles of 32 x ty: the halo box
 // (read as the current field) and the own tile (previous field).
 bool fast_encode_pair_maps(const float2 *buf, long long sx, long long sy, long long sz,

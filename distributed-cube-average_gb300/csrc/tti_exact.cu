@@ -5,8 +5,8 @@
 // intrinsics so that nothing is contracted into an FMA:
 //   der2      include/derivatives.h:47-54   (9-point second derivative)
 //   derCross  include/derivatives.h:56-91   (64-point direct cross sum)
-//   update    include/sample_compute.h:229-275 (sample_compute) or
-//             include/sample_compute.h:51-101  (sample_compute_optimized,
+//   update    include/sample_compute.h:106-185 (sample_compute) or
+//             include/sample_compute.h:21-102  (sample_compute_optimized,
 //             the vpz/vsv medium form with constant angles).
 // Results are bit-identical to the reference's OpenMP path built without
 // FMA contraction (and to its CUDA arithmetic executed the same way).

@@ -47,6 +47,7 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 
 #include "dc_internal.h"
 #include "dc_ptx.cuh"
@@ -513,6 +514,16 @@ done:
   return true;
 }
 
+// CTAs per SM the register allocation must allow: three of 192 threads
+// (tile rows 6, narrow coefficient forms only), two of 256, one of 512.
+template <int NT>
+constexpr int kMinBlocks = NT <= 192 ? 3 : (NT <= 256 ? 2 : 1);
+
+// Tile rows 6 exist for the FP16/BF16 coefficient forms only: their stages
+// are small enough for three CTAs per SM.
+template <int TY, int CF>
+constexpr bool kTileForm = TY != 6 || CF == CF_F16 || CF == CF_BF16;
+
 // No static shared memory in these kernels: the dynamic window starts at
 // the CTA's shared base, so the 1024-byte alignment holds and every access
 // is a shared-space access.  TMA destinations must be 128-byte aligned; the
@@ -520,7 +531,7 @@ done:
 
 // One pass over a box: CTA (bx, by, bz) sweeps tile (bx, by), z-chunk bz.
 template <int TX, int TY, int CF, bool SPONGE, bool ISO>
-__global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
+__global__ void __launch_bounds__(TX *TY, kMinBlocks<TX * TY>)
     fast_kernel(const __grid_constant__ CUtensorMap tm_cur,
                 const __grid_constant__ CUtensorMap tm_prev,
                 const __grid_constant__ CUtensorMap tm_l,
@@ -545,7 +556,7 @@ __global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
 // item is found from the per-shot prefix counts, so every index here is
 // CTA-uniform.
 template <int TX, int TY, int CF, bool SPONGE, bool ISO>
-__global__ void __launch_bounds__(TX *TY, (TX * TY <= 256) ? 2 : 1)
+__global__ void __launch_bounds__(TX *TY, kMinBlocks<TX * TY>)
     batch_kernel(const __grid_constant__ BatchLaunch bl) {
   extern __shared__ __align__(1024) unsigned char smem[];
   if (smem_u32(smem) & 127u) {
@@ -619,30 +630,50 @@ cudaError_t launch_cf(Sim *sim, const StepParams &prm, int cur, int prev) {
 template <int TY>
 cudaError_t launch_ty(Sim *sim, const StepParams &prm, int cur, int prev) {
   switch (sim->coef_form) {
-    case CF_VV: return launch_cf<TY, CF_VV>(sim, prm, cur, prev);
     case CF_F16: return launch_cf<TY, CF_F16>(sim, prm, cur, prev);
     case CF_BF16: return launch_cf<TY, CF_BF16>(sim, prm, cur, prev);
-    default: return launch_cf<TY, CF_F32>(sim, prm, cur, prev);
+    default: break;
+  }
+  if constexpr (TY == 6) {
+    return cudaErrorInvalidValue;  // tile rows 6: narrow forms only
+  } else {
+    if (sim->coef_form == CF_VV) return launch_cf<TY, CF_VV>(sim, prm, cur, prev);
+    return launch_cf<TY, CF_F32>(sim, prm, cur, prev);
   }
 }
 
 template <int TY>
 cudaError_t set_attrs(int form) {
   switch (form) {
-    case CF_VV: return set_smem_attr_all<TY, CF_VV>();
     case CF_F16: return set_smem_attr_all<TY, CF_F16>();
     case CF_BF16: return set_smem_attr_all<TY, CF_BF16>();
-    default: return set_smem_attr_all<TY, CF_F32>();
+    default: break;
+  }
+  if constexpr (TY == 6) {
+    return cudaErrorInvalidValue;
+  } else {
+    if (form == CF_VV) return set_smem_attr_all<TY, CF_VV>();
+    return set_smem_attr_all<TY, CF_F32>();
   }
 }
 
-// 32 x 8 tiles with two CTAs per SM measured fastest on GB300 (616^3 cube:
-// 2.83 ms per step vs 3.09 ms for 32 x 16); DC_GB300_FAST_TY=16 selects the
-// other.
-int chosen_ty() {
+// 32 x 8 tiles with two CTAs per SM measured fastest on GB300 for the FP32
+// forms (616^3 cube: 2.83 ms per step vs 3.09 ms for 32 x 16).
+// DC_GB300_FAST_TY=16 selects 32 x 16; DC_GB300_FAST_TY=6 selects 32 x 6
+// with three CTAs per SM for the FP16/BF16 forms (the FP32 forms keep 8).
+int chosen_ty(int form) {
   const char *e = std::getenv("DC_GB300_FAST_TY");
   const int v = e ? std::atoi(e) : 0;
-  return v == 16 ? 16 : 8;
+  if (v == 16) return 16;
+  if (v == 6 && (form == CF_F16 || form == CF_BF16)) return 6;
+  return 8;
+}
+
+template <typename F>
+auto by_ty(int ty, F &&f) {
+  if (ty == 16) return f(std::integral_constant<int, 16>{});
+  if (ty == 6) return f(std::integral_constant<int, 6>{});
+  return f(std::integral_constant<int, 8>{});
 }
 
 }  // namespace
@@ -650,7 +681,7 @@ int chosen_ty() {
 FastShape fast_shape(const Sim *sim) {
   // z-chunk: enough CTAs for several waves over 152 SMs while keeping the
   // 8-plane warm-up of each chunk small.
-  const int ty = sim->maps_ty ? sim->maps_ty : chosen_ty();
+  const int ty = sim->maps_ty ? sim->maps_ty : chosen_ty(sim->coef_form);
   const long long tiles = ((sim->sx - 8 + kTX - 1) / kTX + 1) *
                           ((sim->sy - 8 + ty - 1) / ty);
   const long long nzc = sim->sz - 8;
@@ -661,7 +692,7 @@ FastShape fast_shape(const Sim *sim) {
   return FastShape{kTX, ty, static_cast<int>(zc)};
 }
 
-int fast_default_ty() { return chosen_ty(); }
+int fast_default_ty(int form) { return chosen_ty(form); }
 
 bool fast_encode_pair_maps(const float2 *buf, long long sx, long long sy, long long sz,
                            long long pitch, int ty, CUtensorMap *halo, CUtensorMap *own,
@@ -718,8 +749,8 @@ bool fast_encode_medium_maps(int form, const float *coef, const void *coef16, co
 bool fast_encode_maps(Sim *sim, std::string *err) {
   // dynamic shared memory above 48 KB must be enabled per kernel and device
   // (done here, before any stream capture)
-  const int kTY = chosen_ty();
-  cudaError_t ae = kTY == 16 ? set_attrs<16>(sim->coef_form) : set_attrs<8>(sim->coef_form);
+  const int kTY = chosen_ty(sim->coef_form);
+  cudaError_t ae = by_ty(kTY, [&](auto t) { return set_attrs<decltype(t)::value>(sim->coef_form); });
   if (ae != cudaSuccess) {
     *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(ae);
     return false;
@@ -765,8 +796,13 @@ cudaError_t batch_attr_ty(int form) {
   switch (form) {
     case CF_F16: return batch_attr_cf<TY, CF_F16>();
     case CF_BF16: return batch_attr_cf<TY, CF_BF16>();
-    case CF_VV: return batch_attr_cf<TY, CF_VV>();
-    default: return batch_attr_cf<TY, CF_F32>();
+    default: break;
+  }
+  if constexpr (TY == 6) {
+    return cudaErrorInvalidValue;
+  } else {
+    if (form == CF_VV) return batch_attr_cf<TY, CF_VV>();
+    return batch_attr_cf<TY, CF_F32>();
   }
 }
 
@@ -793,8 +829,13 @@ int batch_occ_ty(int form, bool iso, bool sponge) {
   switch (form) {
     case CF_F16: return batch_occ_cf<TY, CF_F16>(iso, sponge);
     case CF_BF16: return batch_occ_cf<TY, CF_BF16>(iso, sponge);
-    case CF_VV: return batch_occ_cf<TY, CF_VV>(iso, sponge);
-    default: return batch_occ_cf<TY, CF_F32>(iso, sponge);
+    default: break;
+  }
+  if constexpr (TY == 6) {
+    return 0;
+  } else {
+    if (form == CF_VV) return batch_occ_cf<TY, CF_VV>(iso, sponge);
+    return batch_occ_cf<TY, CF_F32>(iso, sponge);
   }
 }
 
@@ -823,30 +864,41 @@ cudaError_t launch_batch_ty(cudaStream_t st, const BatchLaunch &bl, int form, bo
   switch (form) {
     case CF_F16: return launch_batch_cf<TY, CF_F16>(st, bl, iso, sponge, blocks);
     case CF_BF16: return launch_batch_cf<TY, CF_BF16>(st, bl, iso, sponge, blocks);
-    case CF_VV: return launch_batch_cf<TY, CF_VV>(st, bl, iso, sponge, blocks);
-    default: return launch_batch_cf<TY, CF_F32>(st, bl, iso, sponge, blocks);
+    default: break;
+  }
+  if constexpr (TY == 6) {
+    return cudaErrorInvalidValue;
+  } else {
+    if (form == CF_VV) return launch_batch_cf<TY, CF_VV>(st, bl, iso, sponge, blocks);
+    return launch_batch_cf<TY, CF_F32>(st, bl, iso, sponge, blocks);
   }
 }
 
 }  // namespace
 
+bool fast_tile_rows_valid(int ty, int form) {
+  return ty == 8 || ty == 16 || (ty == 6 && (form == CF_F16 || form == CF_BF16));
+}
+
 cudaError_t batch_prepare(int ty, int form) {
-  return ty == 16 ? batch_attr_ty<16>(form) : batch_attr_ty<8>(form);
+  return by_ty(ty, [&](auto t) { return batch_attr_ty<decltype(t)::value>(form); });
 }
 
 int batch_blocks_per_sm(int ty, int form, bool iso, bool sponge) {
-  return ty == 16 ? batch_occ_ty<16>(form, iso, sponge) : batch_occ_ty<8>(form, iso, sponge);
+  return by_ty(ty, [&](auto t) { return batch_occ_ty<decltype(t)::value>(form, iso, sponge); });
 }
 
 cudaError_t launch_batch(cudaStream_t st, const BatchLaunch &bl, int ty, int form, bool iso,
                          bool sponge, int blocks) {
-  return ty == 16 ? launch_batch_ty<16>(st, bl, form, iso, sponge, blocks)
-                  : launch_batch_ty<8>(st, bl, form, iso, sponge, blocks);
+  return by_ty(ty, [&](auto t) {
+    return launch_batch_ty<decltype(t)::value>(st, bl, form, iso, sponge, blocks);
+  });
 }
 
 cudaError_t launch_fast(Sim *sim, const StepParams &prm, int cur_buf, int prev_buf) {
-  if (sim->maps_ty == 16) return launch_ty<16>(sim, prm, cur_buf, prev_buf);
-  return launch_ty<8>(sim, prm, cur_buf, prev_buf);
+  return by_ty(sim->maps_ty, [&](auto t) {
+    return launch_ty<decltype(t)::value>(sim, prm, cur_buf, prev_buf);
+  });
 }
 
 }  // namespace dcg

@@ -547,8 +547,10 @@ int dc_gb300_lb_rollout(dc_gb300_sim *wide, dc_gb300_sim *thin, const long offse
  * 33 KB file-scope scratch array per device (per-step energy accumulators
  * and a step counter).  The first call on a device looks up its address
  * (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  Each call clears the part of the scratch it uses; all calls on
- * a device share it, so calls that overlap on the GPU race. */
+ * capture.  The address is kept for the life of the process: a
+ * cudaDeviceReset between calls is not supported.  Each call clears the
+ * part of the scratch it uses; all calls on a device share it, so calls
+ * that overlap on the GPU race. */
 int dc_gb300_exact_steps_noalloc(const dc_gb300_config *cfg, float *pairs[2],
                                  const float *medium, int steps, double *energy,
                                  void *stream);

@@ -24,9 +24,9 @@
   ``-DREF_DEVICE_BACKEND``): the reference's own GPU path, for the parity
   gate and the GPU-to-GPU comparison.
 
-This file is the only one that names the location of the reference
-checkout (``DC_REFERENCE_ROOT``, default the container's mount point); all
-other code reads the staged copy or the built libraries.
+The checkout is located by the environment variable ``DC_REFERENCE_ROOT``
+alone; without it the staged copy is used where one exists.  Stage once
+with ``DC_REFERENCE_ROOT=<checkout> python oracle/build_oracle.py``.
 """
 from __future__ import annotations
 
@@ -45,7 +45,8 @@ REF_SO = REF_DIR / "libref.so"
 REF_NATIVE_SO = REF_DIR / "librefomp.so"
 REF_CUDA_SO = REF_DIR / "librefcuda.so"
 REF_OBJ = REF_DIR / "obj"
-REFERENCE_ROOT = Path(os.environ.get("DC_REFERENCE_ROOT", "/root/reference"))
+_ROOT_ENV = os.environ.get("DC_REFERENCE_ROOT")
+REFERENCE_ROOT = Path(_ROOT_ENV) if _ROOT_ENV else None
 
 # The reference files on the propagation path that build without MPI.
 REF_SOURCES = (
@@ -97,7 +98,9 @@ def build_port(force: bool = False) -> Path:
     return PORT_SO
 
 
-def _has_all(root: Path) -> bool:
+def _has_all(root: Path | None) -> bool:
+    if root is None:
+        return False
     files = REF_SOURCES + REF_CUDA_SOURCES
     return all((root / s).is_file() for s in files) and (root / "include").is_dir()
 

@@ -54,7 +54,7 @@ static void init_coefs(void) {
 /* ---- type-generic stencil ------------------------------------------------
  * The body below is instantiated for float (T=float) and double (T=double).
  * Operation order follows include/derivatives.h:47-91 and
- * include/sample_compute.h:196-276 exactly: C evaluates + and - left to
+ * include/sample_compute.h:106-185 exactly: C evaluates + and - left to
  * right, so each accumulation below is the reference's expression tree.   */
 
 #define O_DEFINE_STENCIL(T, SUF, KK, LAB)                                      \
@@ -105,7 +105,7 @@ static const float kRefCudaCh[6] = {0.1459632909f, 0.3540367091f, 0.5f,
                                     0.5403023059f};
 static const float kRefCudaV2px = 1.48f, kRefCudaV2pn = 1.2f;
 
-/* The p/q update at one point, include/sample_compute.h:229-275
+/* The p/q update at one point, include/sample_compute.h:106-185
  * (sample_compute), float.  g is the sponge factor (1 in the interior, where
  * the update reduces exactly to the reference's). */
 static inline void point_f32(long i, long sX, long sY, long sZ,
@@ -224,7 +224,7 @@ int o_step(int kind, long sx, long sy, long sz, const long b0[3],
     if (b0[d] < lo[d] || b1[d] > hi[d]) return -1;
   }
   const long sX = 1, sY = sx, sZ = sx * sy;
-  /* include/sample_compute.h:218-224 */
+  /* include/sample_compute.h:128-133 */
   const float finv[6] = {1.0f / (dx * dx), 1.0f / (dy * dy), 1.0f / (dz * dz),
                          1.0f / (dx * dy), 1.0f / (dx * dz), 1.0f / (dy * dz)};
   const double dinv[6] = {1.0 / ((double)dx * dx), 1.0 / ((double)dy * dy),

@@ -80,7 +80,7 @@ def test_struct_layouts_match_reference_headers(dc, tmp_path, reference):
     (include/dc_process.h, include/device_data.h), compiled side by side."""
     from oracle import build_oracle
     ours = _layout(tmp_path, [str(dc.HEADER.parent)], "dc_gb300.h")
-    ref_inc = build_oracle.REFERENCE_ROOT / "include"
+    ref_inc = build_oracle.source_root() / "include"
     stub = Path(build_oracle.__file__).resolve().parent / "ref_stub"
     theirs = _layout(tmp_path, [str(ref_inc), str(stub)], "device_data.h")
     assert ours == theirs

@@ -172,6 +172,31 @@ def test_batch_fp16_medium(dc, port, medium_coef):
     assert err <= 1.5e-3
 
 
+@pytest.fixture(scope="module")
+def batch_f16(dc, medium_coef):
+    return run_batch(dc, medium_coef, steps_split=(STEPS,), form=dc.MEDIUM_PRECOMP_F16,
+                     tiles=(8, 1))
+
+
+@pytest.mark.parametrize("tiles,persistent", [((6, 1), True), ((6, 3), False), ((16, 2), True)])
+def test_batch_fp16_tile_rows_do_not_change_results(dc, medium_coef, batch_f16, tiles,
+                                                    persistent):
+    """32 x 6 tiles (three CTAs per SM, FP16/BF16 media only) and the other
+    tile shapes give the same bits as 32 x 8."""
+    other = run_batch(dc, medium_coef, steps_split=(STEPS,), form=dc.MEDIUM_PRECOMP_F16,
+                      tiles=tiles, persistent=persistent)
+    for (a, ta), (b, tb) in zip(batch_f16, other):
+        for k in ("pp", "pc", "qp", "qc"):
+            assert np.array_equal(a[k], b[k]), k
+        assert np.array_equal(ta, tb)
+
+
+def test_batch_rejects_tile_rows_six_for_fp32(dc, medium_coef):
+    with dc.Batch(MEDIUM, D, DT, device=0, max_steps=10) as b:
+        with pytest.raises(dc.DcError):
+            b.set_tiles(6, 1)
+
+
 def test_batch_autotune(dc, medium_coef, batch_f32):
     with dc.Batch(MEDIUM, D, DT, device=0, max_steps=STEPS + 2) as b:
         b.set_precomp(medium_coef)

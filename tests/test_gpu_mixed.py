@@ -5,10 +5,12 @@ terms scaled by 2^-vexp), computes in FP32 and keeps FP32 wavefields.
 * Against the oracle run on identically rounded coefficients the result must
   agree to FP32 reordering noise (rel. L2 <= 1e-5): the kernel adds no error
   beyond the storage rounding.
-* Against the FP64 oracle on the exact coefficients the storage rounding
-  costs, on a 64^3 + 16 layered medium after 300 steps of dt = 0.8 ms:
-  FP16 <= 1.5e-3, BF16 <= 1e-2 (measured on CPU emulation: 7.3e-4 and
-  4.7e-3).
+* Against the FP64 oracle on the exact coefficients, on a 64^3 + 16 layered
+  medium after 300 steps of dt = 0.8 ms, FP16 storage meets the accuracy bar
+  of relative L2 <= 1e-3 (measured 7.3e-4).  BF16 storage does not: its 8
+  mantissa bits on the four velocity terms alone cost 4.4e-3 (all ten
+  coefficients 4.7e-3); the test pins that it stays within (1e-3, 1e-2] so
+  that the miss is stated, not hidden behind a loose bound.
 """
 import math
 
@@ -61,8 +63,11 @@ def layered_case(dc, port):
     return geom, coef, steps, dt, src, sponge, s_idx, f64
 
 
-@pytest.mark.parametrize("fmt,medium_form,bound", [("f16", 2, 1.5e-3), ("bf16", 3, 1e-2)])
-def test_mixed_precision_medium(dc, port, layered_case, fmt, medium_form, bound):
+BAR = 1e-3  # relative L2 against the FP64 oracle
+
+
+@pytest.mark.parametrize("fmt,medium_form", [("f16", 2), ("bf16", 3)])
+def test_mixed_precision_medium(dc, port, layered_case, fmt, medium_form):
     geom, coef, steps, dt, src, sponge, s_idx, f64 = layered_case
     with dc.Simulation(geom.sizes, (12.5,) * 3, dt, kernel=dc.KERNEL_FAST, medium=medium_form,
                        device=0) as sim:
@@ -79,7 +84,10 @@ def test_mixed_precision_medium(dc, port, layered_case, fmt, medium_form, bound)
     assert rel_l2(out["pc"], emu.pc) <= 1e-5 and rel_l2(out["qc"], emu.qc) <= 1e-5
     err = rel_l2(out["pc"], f64.pc)
     print(f"{fmt}: rel L2 vs FP64 oracle after {steps} steps = {err:.3e}")
-    assert err <= bound
+    if fmt == "f16":
+        assert err <= BAR
+    else:  # BF16 misses the bar (see the module docstring)
+        assert BAR < err <= 1e-2
 
 
 def test_mixed_precision_keeps_fp32_for_exact_kernel(dc, port, layered_case):
@@ -98,3 +106,25 @@ def test_mixed_precision_keeps_fp32_for_exact_kernel(dc, port, layered_case):
     ref = port.run(KIND_F32, geom.sizes, (12.5,) * 3, dt, n, *z, coef=coef, src_index=s_idx,
                    src=src)
     assert np.array_equal(out["pc"], ref.pc)
+
+
+@pytest.mark.parametrize("medium_form", [2, 3])
+def test_tile_rows_six_bit_identical(dc, layered_case, monkeypatch, medium_form):
+    """DC_GB300_FAST_TY=6 (32 x 6 tiles, three CTAs per SM) on the FP16/BF16
+    forms gives the same bits as the default 32 x 8 tiles."""
+    geom, coef, steps, dt, src, sponge, s_idx, f64 = layered_case
+    n = 60
+    out = {}
+    for ty in ("8", "6"):
+        monkeypatch.setenv("DC_GB300_FAST_TY", ty)
+        with dc.Simulation(geom.sizes, (12.5,) * 3, dt, kernel=dc.KERNEL_FAST,
+                           medium=medium_form, device=0) as sim:
+            sim.set_precomp(coef)
+            sim.set_fields()
+            sim.set_source(s_idx, src)
+            sim.set_sponge(*sponge)
+            sim.run(n)
+            sim.synchronize()
+            out[ty] = sim.get_fields()
+    for k in ("pp", "pc", "qp", "qc"):
+        assert np.array_equal(out["8"][k], out["6"][k]), k

@@ -1,8 +1,15 @@
 """dc_gb300_exact_steps_noalloc: the exact stencil over caller-owned device
-buffers, no device allocation.  Checked through the C ABI against the
-simulation entry points (dc_gb300_run with the exact kernel) on two calls in
-a row, within the tolerance of the parity tests (relative L2 <= 1e-5 for the
-fields, relative difference <= 1e-5 for each step's energy).
+buffers, for callers that cannot allocate device memory themselves (their
+memory is all owned up front, or their time loop must not allocate).
+Checked through the C ABI on two calls in a row, for both medium forms and
+with and without the energy output:
+
+* against the simulation entry points (dc_gb300_run with the exact kernel),
+  within the tolerance of the parity tests (relative L2 <= 1e-5 for the
+  fields, relative difference <= 1e-5 for each step's energy);
+* against the CPU oracle running the reference arithmetic, bit for bit (the
+  exact kernel keeps the reference's operation order);
+* free device memory (cudaMemGetInfo) is the same before and after a call.
 
 The file is named so that pytest collects it last; it also passes alone in a
 fresh process, where its first call does the per-device scratch set-up."""
@@ -53,31 +60,46 @@ def _unpair(buf, shape, pitch):
     return np.ascontiguousarray(a[..., 0]), np.ascontiguousarray(a[..., 1])
 
 
-def _config(dc, sizes, d, dt):
+def _config(dc, sizes, d, dt, medium):
     return dc.Config(sizes[0], sizes[1], sizes[2], d[0], d[1], d[2], dt, dc.KERNEL_EXACT,
-                     dc.MEDIUM_PRECOMP, 0)
+                     medium, 0)
 
 
-def _inputs():
-    g = dict(np.load(GOLDEN / "hetero.npz"))
-    sizes = tuple(int(v) for v in g["sizes"])
-    coef = [g[f"coef{k}"] for k in range(10)]
-    shape = (sizes[2], sizes[1], sizes[0])
-    rng = np.random.default_rng(7)
+def _fields(shape, seed=7):
+    rng = np.random.default_rng(seed)
     fields = [rng.standard_normal(shape).astype(np.float32) for _ in range(4)]
     for f in fields:  # the 4-cell halo stays zero, as in the reference
         f[:4], f[-4:], f[:, :4], f[:, -4:], f[:, :, :4], f[:, :, -4:] = 0, 0, 0, 0, 0, 0
-    return sizes, tuple(float(v) for v in g["d"]), float(g["dt"]), coef, fields
+    return fields
 
 
-def test_noalloc_matches_simulation_on_two_calls(dc):
+def _inputs(medium: str):
+    """Sizes, spacing, dt, the medium (ten coefficients or (vpz, vsv)) and
+    random initial fields: the golden heterogeneous medium for the
+    coefficient form, the golden default medium with its random velocity
+    boundary for the vpz/vsv form."""
+    g = dict(np.load(GOLDEN / ("hetero.npz" if medium == "precomp" else "default_rvb.npz")))
+    sizes = tuple(int(v) for v in g["sizes"])
+    shape = (sizes[2], sizes[1], sizes[0])
+    med = ([g[f"coef{k}"] for k in range(10)] if medium == "precomp"
+           else (g["vpz"], g["vsv"]))
+    return sizes, tuple(float(v) for v in g["d"]), float(g["dt"]), med, _fields(shape)
+
+
+@pytest.mark.parametrize("with_energy", [True, False])
+@pytest.mark.parametrize("medium", ["precomp", "vpz_vsv"])
+def test_noalloc_matches_simulation_and_oracle_on_two_calls(dc, port, medium, with_energy):
     torch = pytest.importorskip("torch")
-    sizes, d, dt, coef, (pp, pc, qp, qc) = _inputs()
+    from oracle.oracle import KIND_F32, KIND_F32_REFCUDA
+    sizes, d, dt, med, (pp, pc, qp, qc) = _inputs(medium)
+    form = dc.MEDIUM_PRECOMP if medium == "precomp" else dc.MEDIUM_VPZ_VSV
     n = 12
     # existing entry points: a simulation running 2n steps with energy
-    with dc.Simulation(sizes, d, dt, kernel=dc.KERNEL_EXACT, medium=dc.MEDIUM_PRECOMP,
-                       device=0) as sim:
-        sim.set_precomp(coef)
+    with dc.Simulation(sizes, d, dt, kernel=dc.KERNEL_EXACT, medium=form, device=0) as sim:
+        if medium == "precomp":
+            sim.set_precomp(med)
+        else:
+            sim.set_vpz_vsv(*med)
         sim.set_fields(pp, pc, qp, qc)
         sim.enable_energy(2 * n)
         sim.run(n)
@@ -87,6 +109,16 @@ def test_noalloc_matches_simulation_on_two_calls(dc):
         sim.synchronize()
         want.append(sim.get_fields())
         want_e = sim.energy(2 * n)
+    # the CPU oracle with the reference arithmetic, n steps at a time
+    kind = KIND_F32 if medium == "precomp" else KIND_F32_REFCUDA
+    o = [a.copy() for a in (pp, pc, qp, qc)]
+    oracle = []
+    for _ in range(2):
+        r = port.run(kind, sizes, d, dt, n, *o, coef=med if medium == "precomp" else None,
+                     vpz=None if medium == "precomp" else med[0],
+                     vsv=None if medium == "precomp" else med[1], energy=True)
+        oracle.append(r)
+        o = [r.pp.copy(), r.pc.copy(), r.qp.copy(), r.qc.copy()]
 
     # caller-owned device buffers (allocated here by the test, not by the
     # entry point)
@@ -95,18 +127,21 @@ def test_noalloc_matches_simulation_on_two_calls(dc):
     dev = torch.device("cuda", 0)
     prev = torch.from_numpy(_pairs(pp, qp, pitch)).to(dev)
     cur = torch.from_numpy(_pairs(pc, qc, pitch)).to(dev)
-    medium = torch.from_numpy(_grouped(coef, pitch)).to(dev)
+    host_medium = _grouped(med, pitch) if medium == "precomp" else _pairs(*med, pitch)
+    medium_dev = torch.from_numpy(host_medium).to(dev)
     torch.cuda.synchronize()
     by_ptr = {prev.data_ptr(): prev, cur.data_ptr(): cur}
-    cfg = _config(dc, sizes, d, dt)
+    cfg = _config(dc, sizes, d, dt, form)
     pairs = (C.c_void_p * 2)(prev.data_ptr(), cur.data_ptr())
     lib = dc.lib()
     for call in range(2):
-        energy = np.zeros(n, np.float64)
+        energy = np.zeros(n, np.float64) if with_energy else None
+        free_before = torch.cuda.mem_get_info(0)[0]
         rc = lib.dc_gb300_exact_steps_noalloc(
-            C.byref(cfg), pairs, C.c_void_p(medium.data_ptr()), n,
-            energy.ctypes.data_as(C.POINTER(C.c_double)), None)
+            C.byref(cfg), pairs, C.c_void_p(medium_dev.data_ptr()), n,
+            energy.ctypes.data_as(C.POINTER(C.c_double)) if with_energy else None, None)
         assert rc == 0, lib.dc_gb300_last_error().decode()
+        assert torch.cuda.mem_get_info(0)[0] == free_before, "device memory changed"
         newest = by_ptr[pairs[1]].cpu().numpy()
         before = by_ptr[pairs[0]].cpu().numpy()
         p_new, q_new = _unpair(newest, shape, pitch)
@@ -114,14 +149,19 @@ def test_noalloc_matches_simulation_on_two_calls(dc):
         w = want[call]
         assert rel_l2(p_new, w["pc"]) <= TOL and rel_l2(q_new, w["qc"]) <= TOL
         assert rel_l2(p_old, w["pp"]) <= TOL and rel_l2(q_old, w["qp"]) <= TOL
-        ref_e = want_e[call * n:(call + 1) * n]
-        assert np.all(ref_e > 0)
-        assert np.max(np.abs(energy - ref_e) / ref_e) <= TOL
+        r = oracle[call]
+        assert np.array_equal(p_new, r.pc) and np.array_equal(q_new, r.qc)
+        assert np.array_equal(p_old, r.pp) and np.array_equal(q_old, r.qp)
+        if with_energy:
+            ref_e = want_e[call * n:(call + 1) * n]
+            assert np.all(ref_e > 0)
+            assert np.max(np.abs(energy - ref_e) / ref_e) <= TOL
+            assert np.max(np.abs(energy - r.energy) / r.energy) <= TOL
 
 
 def test_noalloc_rejects_steps_beyond_scratch(dc):
-    sizes, d, dt, _, _ = _inputs()
-    cfg = _config(dc, sizes, d, dt)
+    sizes, d, dt, _, _ = _inputs("precomp")
+    cfg = _config(dc, sizes, d, dt, dc.MEDIUM_PRECOMP)
     dummy = (C.c_void_p * 2)(16, 32)  # never dereferenced: the count is checked first
     lib = dc.lib()
     rc = lib.dc_gb300_exact_steps_noalloc(C.byref(cfg), dummy, C.c_void_p(48), 4097, None, None)
