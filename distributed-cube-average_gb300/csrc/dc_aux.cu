@@ -356,10 +356,6 @@ __global__ void coef_repitch_kernel(float *coef, const float *gd, long long sx, 
 template <typename H2>
 __device__ __forceinline__ H2 to_h2(float a, float b);
 template <>
-__device__ __forceinline__ __half2 to_h2<__half2>(float a, float b) {
-  return __floats2half2_rn(a, b);
-}
-template <>
 __device__ __forceinline__ __nv_bfloat162 to_h2<__nv_bfloat162>(float a, float b) {
   return __floats2bfloat162_rn(a, b);
 }
@@ -380,7 +376,88 @@ __global__ void coef_narrow_kernel(const float *coef, H2 *hl, H2 *ho1, H2 *ho2, 
   }
 }
 
+// 16-bit fixed point of an angle term (|c| <= 1): q = c x 2^15, round to
+// nearest even, clamped to [-32768, 32767], stored biased as q + 32768; two
+// values per word (first in the low half).
+__device__ __forceinline__ uint32_t pack_fixed(float a, float b) {
+  const int qa = max(-32768, min(32767, __float2int_rn(a * 32768.0f)));
+  const int qb = max(-32768, min(32767, __float2int_rn(b * 32768.0f)));
+  return static_cast<uint32_t>(qa + 32768) | (static_cast<uint32_t>(qb + 32768) << 16);
+}
+
+// FP16 ratio of a velocity term to its row base.
+__device__ __forceinline__ float vratio(float v, float b) {
+  return b != 0.0f ? __fsub_rn(__fdiv_rn(v, b), 1.0f) : 0.0f;
+}
+
+__device__ __forceinline__ uint32_t pack_half(float a, float b) {
+  const __half2 h = __floats2half2_rn(a, b);
+  return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// One warp per medium row: the midrange of the row's non-zero values of
+// each velocity term is its base; then every point of the row (padding
+// included) is encoded.
+__global__ void coef_rowref_kernel(const float *coef, uint32_t *hl, uint32_t *ho1,
+                                   uint32_t *ho2, float4 *vbase, long long rows, long long sx,
+                                   long long pitch, long long count) {
+  const float4 *g0 = reinterpret_cast<const float4 *>(coef);
+  const float4 *g1 = reinterpret_cast<const float4 *>(coef + 4 * count);
+  const float2 *g2 = reinterpret_cast<const float2 *>(coef + 8 * count);
+  const int lane = threadIdx.x & 31;
+  const long long nwarps = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+  for (long long r = (blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x) >> 5;
+       r < rows; r += nwarps) {
+    const long long row = r * pitch;
+    float mn[4], mx[4];
+    for (int k = 0; k < 4; ++k) {
+      mn[k] = INFINITY;
+      mx[k] = -INFINITY;
+    }
+    for (long long x = lane; x < sx; x += 32) {
+      const float4 a = g1[row + x];
+      const float2 b = g2[row + x];
+      const float v[4] = {a.z, a.w, b.x, b.y};
+      for (int k = 0; k < 4; ++k)
+        if (v[k] != 0.0f) {
+          mn[k] = fminf(mn[k], v[k]);
+          mx[k] = fmaxf(mx[k], v[k]);
+        }
+    }
+    float bs[4];
+    for (int k = 0; k < 4; ++k) {
+      for (int off = 16; off > 0; off >>= 1) {
+        mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
+        mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
+      }
+      bs[k] = mn[k] <= mx[k] ? 0.5f * (mn[k] + mx[k]) : 0.0f;
+    }
+    if (lane == 0) vbase[r] = make_float4(bs[0], bs[1], bs[2], bs[3]);
+    for (long long x = lane; x < pitch; x += 32) {
+      const long long i = row + x;
+      const float4 c0 = g0[i], c1 = g1[i];
+      const float2 c2 = g2[i];
+      hl[2 * i] = pack_fixed(c0.x, c0.y);      // cxx, cyy
+      hl[2 * i + 1] = pack_fixed(c0.z, c0.w);  // cxy, czz
+      ho1[2 * i] = pack_fixed(c1.x, c1.y);     // cxz, cyz
+      ho1[2 * i + 1] = pack_half(vratio(c1.z, bs[0]), vratio(c1.w, bs[1]));  // v2px, v2pz
+      ho2[i] = pack_half(vratio(c2.x, bs[2]), vratio(c2.y, bs[3]));          // v2sz, v2pn
+    }
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_coef_rowref(cudaStream_t st, const float *coef, void *coef16, float4 *vbase,
+                               long long sx, long long sy, long long sz, long long pitch,
+                               long long count) {
+  const long long rows = sy * sz;
+  const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((rows + 7) / 8, 152 * 32)));
+  uint32_t *h = static_cast<uint32_t *>(coef16);
+  coef_rowref_kernel<<<blocks, 256, 0, st>>>(coef, h, h + 2 * count, h + 4 * count, vbase, rows,
+                                             sx, pitch, count);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_coef_component(cudaStream_t st, float *coef, float *dense, int k,
                                   long long sx, long long sy, long long sz, long long pitch,
@@ -421,16 +498,12 @@ cudaError_t launch_coef_narrow(cudaStream_t st, const float *coef, void *coef16,
   const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((count + 255) / 256, 152 * 32)));
   const float vscale = ldexpf(1.0f, -vexp);
   // layout: [count] x 8 B (cxx, cyy, cxy, czz), [count] x 8 B (cxz, cyz,
-  // v2px, v2pz), [count] x 4 B (v2sz, v2pn)
-  if (form == CF_F16) {
-    __half2 *h = static_cast<__half2 *>(coef16);
-    coef_narrow_kernel<__half2><<<blocks, 256, 0, st>>>(coef, h, h + 2 * count, h + 4 * count,
-                                                        vscale, count);
-  } else {
-    __nv_bfloat162 *h = static_cast<__nv_bfloat162 *>(coef16);
-    coef_narrow_kernel<__nv_bfloat162><<<blocks, 256, 0, st>>>(coef, h, h + 2 * count,
-                                                               h + 4 * count, vscale, count);
-  }
+  // v2px, v2pz), [count] x 4 B (v2sz, v2pn); the FP16 form has its own
+  // encoding (launch_coef_rowref)
+  if (form != CF_BF16) return cudaErrorInvalidValue;
+  __nv_bfloat162 *h = static_cast<__nv_bfloat162 *>(coef16);
+  coef_narrow_kernel<__nv_bfloat162><<<blocks, 256, 0, st>>>(coef, h, h + 2 * count,
+                                                             h + 4 * count, vscale, count);
   return cudaGetLastError();
 }
 

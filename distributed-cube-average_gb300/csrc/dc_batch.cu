@@ -54,6 +54,7 @@ struct Batch {
   bool medium_set = false, narrow_stale = true;
   float *coef = nullptr;   // grouped FP32 coefficients of the medium box
   void *coef16 = nullptr;  // FP16/BF16 copy (narrow forms)
+  float4 *vbase = nullptr; // FP16 form: velocity bases per medium row
   int max_steps = 0;
   std::vector<BShot> shots;
   // device tables (rebuilt by prepare)
@@ -175,16 +176,28 @@ void release(Batch *b) {
   if (b->side) cudaStreamDestroy(b->side);
   cudaFree(b->coef);
   cudaFree(b->coef16);
+  cudaFree(b->vbase);
   cudaFree(b->d_step);
   cudaFree(b->d_err);
   if (b->stream) cudaStreamDestroy(b->stream);
 }
 
-// FP16/BF16 copy of the medium with the velocity terms scaled by 2^-vexp
-// (the same rule as a single-shot simulation).
+// The 16-bit copy of the medium (the same encodings as a single-shot
+// simulation): FP16 with per-row velocity bases, or BF16 with the velocity
+// terms scaled by 2^-vexp.
 int refresh_narrow(Batch *b) {
   if (!(b->coef_form == CF_F16 || b->coef_form == CF_BF16) || !b->narrow_stale)
     return DC_GB300_OK;
+  if (b->coef_form == CF_F16) {
+    BATCH_TRY(launch_coef_rowref(b->stream, b->coef, b->coef16, b->vbase, b->mx, b->my, b->mz,
+                                 b->mpitch, b->mcount));
+    BATCH_TRY(cudaStreamSynchronize(b->stream));
+    b->vexp = 0;
+    b->narrow_stale = false;
+    b->prepared = false;
+    drop_graphs(b);
+    return DC_GB300_OK;
+  }
   unsigned int *d_max = nullptr;
   unsigned int bits = 0;
   BATCH_TRY(cudaMalloc(&d_max, sizeof(unsigned int)));
@@ -222,9 +235,9 @@ int prepare(Batch *b, int ty, int zsplit, bool persistent) {
   b->persistent = persistent;
   const int n = static_cast<int>(b->shots.size());
   std::string err;
-  CUtensorMap tm_c[3];
-  if (!fast_encode_medium_maps(b->coef_form, b->coef, b->coef16, nullptr, b->mx, b->my, b->mz,
-                               b->mpitch, b->mcount, ty, tm_c, &err))
+  CUtensorMap tm_c[4];
+  if (!fast_encode_medium_maps(b->coef_form, b->coef, b->coef16, nullptr, b->vbase, b->mx,
+                               b->my, b->mz, b->mpitch, b->mcount, ty, tm_c, &err))
     return fail(DC_GB300_ERR_CUDA, err);
   std::vector<CUtensorMap> maps(static_cast<size_t>(n) * 4);
   for (int i = 0; i < n; ++i) {
@@ -286,7 +299,7 @@ int prepare(Batch *b, int ty, int zsplit, bool persistent) {
   // launch parameters, one group per kMaxBatchShots shots
   StepParams common{};
   fill_weights(&common, b->dx, b->dy, b->dz, b->dt);
-  if (b->coef_form == CF_F16 || b->coef_form == CF_BF16) {
+  if (b->coef_form == CF_BF16) {
     common.dt2 = ldexpf(common.dt2, b->vexp);
     common.dt2_iso = ldexpf(common.dt2_iso, b->vexp);
   }
@@ -314,6 +327,7 @@ int prepare(Batch *b, int ty, int zsplit, bool persistent) {
     bl.tm_l = tm_c[0];
     bl.tm_o1 = tm_c[1];
     bl.tm_o2 = tm_c[2];
+    bl.tm_vb = tm_c[3];
     bl.maps = b->d_maps + 4 * g0;
     bl.nshots = span.second - g0;
     b->group_first.push_back(g0);
@@ -625,6 +639,9 @@ extern "C" int dc_gb300_batch_create(const dc_gb300_batch_config *cfg, dc_gb300_
     return bail(DC_GB300_ERR_NOMEM, "medium coefficients");
   if (b->coef_form != dcg::CF_F32 && cudaMalloc(&b->coef16, 20 * b->mcount) != cudaSuccess)
     return bail(DC_GB300_ERR_NOMEM, "narrow medium copy");
+  if (b->coef_form == dcg::CF_F16 &&
+      cudaMalloc(&b->vbase, sizeof(float4) * b->my * b->mz) != cudaSuccess)
+    return bail(DC_GB300_ERR_NOMEM, "velocity bases");
   if (cudaMalloc(&b->d_step, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&b->d_err, sizeof(int)) != cudaSuccess)
     return bail(DC_GB300_ERR_NOMEM, "counters");
@@ -856,8 +873,7 @@ extern "C" int dc_gb300_batch_set_tiles(dc_gb300_batch *h, int ty, int zsplit) {
   if (!b) return fail(DC_GB300_ERR_ARG, "null batch");
   if (!dcg::fast_tile_rows_valid(ty, b->coef_form) || zsplit < 1 || zsplit > 64)
     return fail(DC_GB300_ERR_ARG,
-                "tile rows must be 8 or 16 (or 6 with an FP16/BF16 medium) and zsplit in "
-                "[1, 64]");
+                "tile rows must be 8 or 16 and zsplit in [1, 64]");
   BATCH_TRY(cudaSetDevice(b->device));
   b->ty = ty;
   b->zsplit = zsplit;
@@ -872,9 +888,7 @@ extern "C" int dc_gb300_batch_autotune(dc_gb300_batch *h, int steps, int *ty_out
   if (!b) return fail(DC_GB300_ERR_ARG, "null batch");
   if (steps < 1) return fail(DC_GB300_ERR_ARG, "autotune needs at least one step");
   BATCH_TRY(cudaSetDevice(b->device));
-  // tile rows 6 (three CTAs per SM) exist for the FP16/BF16 forms only
-  std::vector<int> tys = {8, 16};
-  if (dcg::fast_tile_rows_valid(6, b->coef_form)) tys.push_back(6);
+  const int tys[2] = {8, 16};
   const int splits[4] = {1, 2, 4, 8};
   int best_ty = b->ty, best_split = b->zsplit;
   bool best_persistent = b->persistent;

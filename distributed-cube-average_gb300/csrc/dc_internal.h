@@ -44,10 +44,15 @@ __host__ __device__ __forceinline__ long long coef_index(int k, long long i, lon
 }
 
 // Reduced-precision copy of the medium for the fast kernel (the mixed
-// form), FP16 or BF16 in three arrays: 8 bytes (cxx, cyy, cxy, czz), 8 bytes
-// (cxz, cyz, v2px, v2pz) and 4 bytes (v2sz, v2pn) per point.  The four
-// velocity terms are stored scaled by 2^-vexp so they stay in FP16's range;
-// the kernel folds 2^vexp into dt^2.
+// form) in three arrays: 8 bytes (cxx, cyy, cxy, czz), 8 bytes (cxz, cyz,
+// v2px, v2pz) and 4 bytes (v2sz, v2pn) per point, 16 bits per value.
+//  * CF_F16: the six angle terms as 16-bit fixed point (value x 2^15,
+//    round to nearest, clamped to [-32768, 32767], stored + 32768); the four
+//    velocity terms
+//    as FP16 ratios d = v / b - 1 to an FP32 base b per medium row (the
+//    midrange of the row's non-zero values), decoded as v = b + b * d.
+//  * CF_BF16: all ten values rounded to BF16, the velocity terms scaled by
+//    2^-vexp; the kernel folds 2^vexp into dt^2.
 enum CoefForm { CF_F32 = 0, CF_VV = 1, CF_F16 = 2, CF_BF16 = 3 };
 // Device slot of each dc_precomp_vars field (reference order ch1dxx, ch1dyy,
 // ch1dzz, ch1dxy, ch1dyz, ch1dxz, v2px, v2pz, v2sz, v2pn).
@@ -110,6 +115,7 @@ struct StepParams {
 constexpr int kMaxBatchShots = 64;
 struct BatchLaunch {
   CUtensorMap tm_l, tm_o1, tm_o2;  // shared medium (coefficient groups)
+  CUtensorMap tm_vb;                // FP16 medium: velocity bases per row
   const CUtensorMap *maps;          // [shot][4]: halo of buffer 0, 1; own tile of buffer 0, 1
   const int *order;                 // launch order of the work items (null: shot by shot)
   int nshots;
@@ -136,6 +142,7 @@ struct Sim {
   float *vv = nullptr;         // (vpz, vsv) pairs
   // reduced-precision copy used by the fast kernel (DC_GB300_MEDIUM_*_F16/BF16)
   void *coef16 = nullptr;      // [count] x 8 B, [count] x 8 B, [count] x 4 B
+  float4 *vbase = nullptr;     // CF_F16: velocity bases per row, [sz][sy]
   int coef_form = CF_F32;      // CoefForm the fast kernel reads
   int vexp = 0;                // velocity terms stored scaled by 2^-vexp
   bool coef16_stale = true;
@@ -164,7 +171,7 @@ struct Sim {
   long long launches = 0;
   int config_version = 0;
   // tensor maps for the fast kernel (encoded for one tile shape)
-  CUtensorMap tm_halo[2], tm_own[2], tm_c[3];
+  CUtensorMap tm_halo[2], tm_own[2], tm_c[4];  // tm_c: L, O1, O2, row bases
   int maps_tx = 0, maps_ty = 0;
   // learned absorbing layer, applied after every stencil pass of a run
   const float *lb_params = nullptr;  // MLP compute parameters (device, owned by the MLP)
@@ -190,10 +197,9 @@ struct FastShape {
 FastShape fast_shape(const Sim *sim);
 bool fast_encode_maps(Sim *sim, std::string *err);
 // Tile rows (TY) of the fast kernel for coefficient form `form`: 8 unless
-// DC_GB300_FAST_TY selects 16, or 6 (FP16/BF16 forms only).
+// DC_GB300_FAST_TY selects 16.
 int fast_default_ty(int form);
-// Whether tile rows `ty` are compiled for coefficient form `form` (8 and 16
-// for every form, 6 for the FP16/BF16 forms).
+// Whether tile rows `ty` are compiled for coefficient form `form` (8 and 16).
 bool fast_tile_rows_valid(int ty, int form);
 // Tensor maps of one (p, q) pair buffer for tiles of 32 x ty: the halo box
 // (read as the current field) and the own tile (previous field).
@@ -201,9 +207,12 @@ bool fast_encode_pair_maps(const float2 *buf, long long sx, long long sy, long l
                            long long pitch, int ty, CUtensorMap *halo, CUtensorMap *own,
                            std::string *err);
 // Tensor maps of the three coefficient groups of a medium in form `form`.
+// out[0..2] = the groups L, O1, O2; out[3] = the FP16 form's row bases
+// (vbase, [sz][sy] float4; a copy of out[2] for the other forms).
 bool fast_encode_medium_maps(int form, const float *coef, const void *coef16, const float *vv,
-                             long long sx, long long sy, long long sz, long long pitch,
-                             long long count, int ty, CUtensorMap out[3], std::string *err);
+                             const float4 *vbase, long long sx, long long sy, long long sz,
+                             long long pitch, long long count, int ty, CUtensorMap out[4],
+                             std::string *err);
 // Batched fast kernel (always with the sponge).  `blocks` = persistent CTAs.
 cudaError_t batch_prepare(int ty, int form);  // shared-memory attributes
 // `sponge` false: every shot's sponge profile is 1 (the no-sponge sweep)
@@ -264,10 +273,16 @@ cudaError_t launch_coef_vmax(cudaStream_t st, const float *coef, long long count
 cudaError_t launch_coef_repitch(cudaStream_t st, float *coef, const float *grouped_dense,
                                 long long sx, long long sy, long long sz, long long pitch,
                                 long long count);
-// FP32 grouped -> FP16/BF16 copy (form CF_F16 or CF_BF16) with velocity
-// terms scaled by 2^-vexp.
+// FP32 grouped -> BF16 copy (form CF_BF16) with velocity terms scaled by
+// 2^-vexp.
 cudaError_t launch_coef_narrow(cudaStream_t st, const float *coef, void *coef16, int form,
                                int vexp, long long count);
+// FP32 grouped -> the CF_F16 copy (fixed-point angle terms, FP16 velocity
+// ratios) and its per-row velocity bases vbase[sz * sy] (rows of sx points
+// at the given pitch).
+cudaError_t launch_coef_rowref(cudaStream_t st, const float *coef, void *coef16, float4 *vbase,
+                               long long sx, long long sy, long long sz, long long pitch,
+                               long long count);
 cudaError_t launch_layered(cudaStream_t st, const dc_gb300_layered_spec &spec,
                            float *coef, float *vv, long long sx, long long sy,
                            long long sz, long long pitch, long long count);

@@ -166,6 +166,7 @@ void release(Sim *s) {
   }
   cudaFree(s->coef);
   cudaFree(s->coef16);
+  cudaFree(s->vbase);
   cudaFree(s->vv);
   cudaFree(s->sponge);
   cudaFree(s->d_src);
@@ -230,8 +231,8 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
   p.pitch = s->pitch;
   p.plane = s->plane;
   fill_weights(&p, dx, dy, dz, dt);
-  // the FP16/BF16 medium stores the velocity terms scaled by 2^-vexp
-  if (s->coef_form == CF_F16 || s->coef_form == CF_BF16) {
+  // the BF16 medium stores the velocity terms scaled by 2^-vexp
+  if (s->coef_form == CF_BF16) {
     p.dt2 = ldexpf(p.dt2, s->vexp);
     p.dt2_iso = ldexpf(p.dt2_iso, s->vexp);
   }
@@ -453,6 +454,10 @@ extern "C" int dc_gb300_create(const dc_gb300_config *cfg, dc_gb300_sim **out) {
     if ((s->coef_form == CF_F16 || s->coef_form == CF_BF16) &&
         cudaMalloc(&s->coef16, static_cast<size_t>(s->count) * 20) != cudaSuccess)
       return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of the FP16 coefficients failed"));
+    if (s->coef_form == CF_F16 &&
+        cudaMalloc(reinterpret_cast<void **>(&s->vbase), sizeof(float4) * s->sy * s->sz) !=
+            cudaSuccess)
+      return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of the velocity bases failed"));
   } else {
     if (cudaMalloc(&s->vv, bytes * 2) != cudaSuccess)
       return bail(fail(DC_GB300_ERR_NOMEM, "cudaMalloc of vpz/vsv failed"));
@@ -648,11 +653,22 @@ int precompute_dense(cudaStream_t st, int dev, const dc_anisotropy_t *a, long lo
   return DC_GB300_OK;
 }
 
-// Refreshes the FP16/BF16 copy of the medium when the fast kernel reads it:
-// the velocity terms are scaled by 2^-vexp so their maximum stays below 2^14.
+// Refreshes the 16-bit copy of the medium when the fast kernel reads it:
+// FP16 with fixed-point angle terms and per-row velocity bases, or BF16 with
+// the velocity terms scaled by 2^-vexp so their maximum stays below 2^14.
 int refresh_narrow(Sim *s) {
   if (!(s->coef_form == CF_F16 || s->coef_form == CF_BF16) || !s->coef16_stale)
     return DC_GB300_OK;
+  if (s->coef_form == CF_F16) {
+    DCG_TRY(launch_coef_rowref(s->stream, s->coef, s->coef16, s->vbase, s->sx, s->sy, s->sz,
+                               s->pitch, s->count));
+    DCG_TRY(cudaStreamSynchronize(s->stream));
+    s->vexp = 0;
+    s->coef16_stale = false;
+    drop_graphs(s);
+    ++s->config_version;
+    return DC_GB300_OK;
+  }
   unsigned int *d_max = nullptr;
   unsigned int bits = 0;
   DCG_TRY(cudaMallocAsync(reinterpret_cast<void **>(&d_max), sizeof(unsigned int), s->stream));

@@ -81,7 +81,10 @@ struct FastLayout {
   static constexpr int OFF_O1 = OFF_L + NT * CB::L;
   static constexpr int OFF_O2 = OFF_O1 + NT * CB::O1;
   static constexpr int OFF_OWN = align128(OFF_O2 + NT * CB::O2);  // (pp, qp) pairs
-  static constexpr int STAGE_BYTES = OFF_OWN + NT * 8;
+  // FP16 form: the velocity bases of the tile's TY rows at the output plane
+  static constexpr int VB = CF == CF_F16 ? 16 : 0;
+  static constexpr int OFF_VB = align128(OFF_OWN + NT * 8);
+  static constexpr int STAGE_BYTES = align128(OFF_VB + TY * VB);
   static constexpr int DY_BYTES = align128(TY * HX * 8);      // y-derivative plane
   static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;         // 3 buffers
   // per-thread ring of the delayed in-plane terms of the last 9 planes:
@@ -92,7 +95,7 @@ struct FastLayout {
   static constexpr int SMEM_BYTES = OFF_BAR + NSTAGE * 8;
   static constexpr uint32_t TX_HALO = HX * HY * 8u;
   static constexpr uint32_t TX_LEAD = NT * CB::L;
-  static constexpr uint32_t TX_OUT = NT * (CB::O1 + CB::O2) + NT * 8u;
+  static constexpr uint32_t TX_OUT = NT * (CB::O1 + CB::O2) + NT * 8u + TY * VB;
   static_assert(TX % 32 == 0, "a warp spans one tile row");
   static_assert(8 * TY <= NT, "halo-column work fits the CTA");
 };
@@ -209,13 +212,31 @@ __device__ __forceinline__ float2 h2f(uint32_t v, bool bf16) {
   return __half22float2(h);
 }
 
+// Two 16-bit fixed-point values (low half first, each stored biased by
+// 2^15) as exact floats: a byte permutation places each half in the low
+// mantissa bits of 2^23, and one packed subtraction of 2^23 + 2^15 removes
+// both offsets.  The values come out scaled by 2^15; the sweep unscales H1
+// once.
+__device__ __forceinline__ float2 fx2f(uint32_t w) {
+  const uint32_t lo = __byte_perm(w, 0x4b000000u, 0x7610);
+  const uint32_t hi = __byte_perm(w, 0x4b000000u, 0x7632);
+  return __fadd2_rn(make_float2(__uint_as_float(lo), __uint_as_float(hi)),
+                    make_float2(-8421376.0f, -8421376.0f));
+}
+
+// Scale of the angle terms as the kernel reads them (1 / 2^15 for the
+// fixed-point FP16 form, applied to H1).
+template <int CF>
+constexpr float kChUnscale = CF == CF_F16 ? 1.0f / 32768.0f : 1.0f;
+
 // (cxx, cyy, cxy, czz) of the thread's point at the leading plane.
 template <int CF>
 __device__ __forceinline__ float4 load_lead(const unsigned char *l, int ot) {
   if (CF == CF_F32) return reinterpret_cast<const float4 *>(l)[ot];
   if (CF == CF_VV) return make_float4(kCxx, kCyy, kCxy, kCzz);
   const uint2 h = reinterpret_cast<const uint2 *>(l)[ot];
-  const float2 a = h2f(h.x, CF == CF_BF16), b = h2f(h.y, CF == CF_BF16);
+  const float2 a = CF == CF_F16 ? fx2f(h.x) : h2f(h.x, true);
+  const float2 b = CF == CF_F16 ? fx2f(h.y) : h2f(h.y, true);
   return make_float4(a.x, a.y, b.x, b.y);
 }
 
@@ -227,7 +248,7 @@ struct OutMedium {
 
 template <int CF>
 __device__ __forceinline__ OutMedium load_out(const unsigned char *o1, const unsigned char *o2,
-                                              int ot) {
+                                              int ot, float4 vb) {
   if (CF == CF_F32) {
     const float4 g1 = reinterpret_cast<const float4 *>(o1)[ot];
     const float2 g2 = reinterpret_cast<const float2 *>(o2)[ot];
@@ -239,10 +260,16 @@ __device__ __forceinline__ OutMedium load_out(const unsigned char *o1, const uns
     const float v2pz = v.x * v.x;
     return OutMedium{kCxz, kCyz, v2pz * kV2pxFactor, v2pz, v.y * v.y, v2pz * kV2pnFactor};
   }
-  const bool bf = CF == CF_BF16;
   const uint2 h = reinterpret_cast<const uint2 *>(o1)[ot];
   const uint32_t h2 = reinterpret_cast<const uint32_t *>(o2)[ot];
-  const float2 a = h2f(h.x, bf), b = h2f(h.y, bf), c = h2f(h2, bf);
+  if (CF == CF_F16) {
+    // fixed-point cxz, cyz (x 2^15); velocity v = b + b * d from the row's
+    // bases vb and the FP16 ratios d
+    const float2 a = fx2f(h.x), b = h2f(h.y, false), c = h2f(h2, false);
+    return OutMedium{a.x, a.y, fmaf(vb.x, b.x, vb.x), fmaf(vb.y, b.y, vb.y),
+                     fmaf(vb.z, c.x, vb.z), fmaf(vb.w, c.y, vb.w)};
+  }
+  const float2 a = h2f(h.x, true), b = h2f(h.y, true), c = h2f(h2, true);
   return OutMedium{a.x, a.y, b.x, b.y, c.x, c.y};
 }
 
@@ -258,7 +285,8 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
                                              const CUtensorMap *tm_prev,
                                              const CUtensorMap *tm_l,
                                              const CUtensorMap *tm_o1,
-                                             const CUtensorMap *tm_o2, const StepParams &prm,
+                                             const CUtensorMap *tm_o2,
+                                             const CUtensorMap *tm_vb, const StepParams &prm,
                                              const StepParams &cw, const int x0, const int y0, const int zb,
                                              const int ze, unsigned char *smem) {
   using Lay = FastLayout<TX, TY, CF>;
@@ -291,6 +319,7 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
     if (CB::L) prefetch_tensormap(tm_l);
     prefetch_tensormap(tm_o1);
     if (CB::O2) prefetch_tensormap(tm_o2);
+    if (Lay::VB) prefetch_tensormap(tm_vb);
   }
   __syncthreads();
 
@@ -314,6 +343,9 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
       const int mz = z + prm.moz;
       tma_load_3d(st + Lay::OFF_O1, tm_o1, XO * mx0, my0, mz, &bars[s]);
       if (CB::O2) tma_load_3d(st + Lay::OFF_O2, tm_o2, mx0, my0, mz, &bars[s]);
+      // FP16 form: rows my0 .. my0 + TY - 1 of the bases (two 8-byte
+      // elements per row)
+      if (Lay::VB) tma_load_2d(st + Lay::OFF_VB, tm_vb, 2 * my0, mz, &bars[s]);
       tma_load_3d(st + Lay::OFF_OWN, tm_prev, x0, y0, z, &bars[s]);
     }
   };
@@ -429,11 +461,16 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
                                dxq[m3], dxq[p3], dxq[m4], dxq[p4]);
           const float2 yz = d1s<ISO, CHAIN>(w1z, dyq[m1], dyq[p1], dyq[m2], dyq[p2],
                                dyq[m3], dyq[p3], dyq[m4], dyq[p4]);
-          const OutMedium md = load_out<CF>(st + Lay::OFF_O1, st + Lay::OFF_O2, ot);
+          // FP16 form: the velocity bases of this thread's row (a broadcast
+          // read: one row per warp)
+          const float4 vb = Lay::VB ? reinterpret_cast<const float4 *>(st + Lay::OFF_VB)[ty]
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+          const OutMedium md = load_out<CF>(st + Lay::OFF_O1, st + Lay::OFF_O2, ot, vb);
           // H1 = sum c * d2 over the six second derivatives; the Laplacian
           // (H1 + H2) = xx + yy + zz
-          const float2 h1 =
+          float2 h1 =
               fma2(bc(md.cyz), yz, fma2(bc(md.cxz), xz, fma2(bc(czz), zz, make_float2(ab.x, ab.y))));
+          if (CF == CF_F16) h1 = mul2(h1, bc(kChUnscale<CF>));
           const float2 h2 = fma2(bc(-1.0f), h1, add2(make_float2(ab.z, ab.w), zz));
           const float rhsp = fmaf(md.v2sz, h1.x - h1.y, fmaf(md.v2pz, h1.y, md.v2px * h2.x));
           const float rhsq = fmaf(-md.v2sz, h2.x - h2.y, fmaf(md.v2pz, h1.y, md.v2pn * h2.x));
@@ -514,15 +551,10 @@ done:
   return true;
 }
 
-// CTAs per SM the register allocation must allow: three of 192 threads
-// (tile rows 6, narrow coefficient forms only), two of 256, one of 512.
+// CTAs per SM the register allocation must allow: two of 256 threads, one
+// of 512.
 template <int NT>
-constexpr int kMinBlocks = NT <= 192 ? 3 : (NT <= 256 ? 2 : 1);
-
-// Tile rows 6 exist for the FP16/BF16 coefficient forms only: their stages
-// are small enough for three CTAs per SM.
-template <int TY, int CF>
-constexpr bool kTileForm = TY != 6 || CF == CF_F16 || CF == CF_BF16;
+constexpr int kMinBlocks = NT <= 256 ? 2 : 1;
 
 // No static shared memory in these kernels: the dynamic window starts at
 // the CTA's shared base, so the 1024-byte alignment holds and every access
@@ -537,6 +569,7 @@ __global__ void __launch_bounds__(TX *TY, kMinBlocks<TX * TY>)
                 const __grid_constant__ CUtensorMap tm_l,
                 const __grid_constant__ CUtensorMap tm_o1,
                 const __grid_constant__ CUtensorMap tm_o2,
+                const __grid_constant__ CUtensorMap tm_vb,
                 const __grid_constant__ StepParams prm) {
   extern __shared__ __align__(1024) unsigned char smem[];
   if (smem_u32(smem) & 127u) {
@@ -547,8 +580,8 @@ __global__ void __launch_bounds__(TX *TY, kMinBlocks<TX * TY>)
   const int y0 = prm.tile_y0 + static_cast<int>(blockIdx.y) * TY;
   const int zb = prm.z0 + static_cast<int>(blockIdx.z) * prm.zchunk;
   const int ze = min(zb + prm.zchunk, prm.z1);
-  sweep_column<TX, TY, CF, SPONGE, ISO>(&tm_cur, &tm_prev, &tm_l, &tm_o1, &tm_o2, prm, prm, x0,
-                                        y0, zb, ze, smem);
+  sweep_column<TX, TY, CF, SPONGE, ISO>(&tm_cur, &tm_prev, &tm_l, &tm_o1, &tm_o2, &tm_vb, prm,
+                                        prm, x0, y0, zb, ze, smem);
 }
 
 // One step of a batch of shots: persistent CTAs stride over the work items
@@ -580,7 +613,8 @@ __global__ void __launch_bounds__(TX *TY, kMinBlocks<TX * TY>)
     // weights, dt2 and energy (none) are the same in every shot: read them
     // from shot 0 at fixed offsets
     if (!sweep_column<TX, TY, CF, SPONGE, ISO>(m + bl.cur_buf, m + 2 + (1 - bl.cur_buf),
-                                             &bl.tm_l, &bl.tm_o1, &bl.tm_o2, prm, bl.shot[0],
+                                             &bl.tm_l, &bl.tm_o1, &bl.tm_o2, &bl.tm_vb, prm,
+                                             bl.shot[0],
                                              x0, y0, zb, ze, smem))
       return;
   }
@@ -599,7 +633,7 @@ cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int cur_buf, int prev
   dim3 grid((nx + kTX - 1) / kTX, (ny + TY - 1) / TY, (nz + prm.zchunk - 1) / prm.zchunk);
   kern<<<grid, kTX * TY, Lay::SMEM_BYTES, sim->stream>>>(
       sim->tm_halo[cur_buf], sim->tm_own[prev_buf], sim->tm_c[0], sim->tm_c[1], sim->tm_c[2],
-      prm);  // tm_c: L, O1, O2
+      sim->tm_c[3], prm);  // tm_c: L, O1, O2, row bases
   return cudaGetLastError();
 }
 
@@ -630,49 +664,36 @@ cudaError_t launch_cf(Sim *sim, const StepParams &prm, int cur, int prev) {
 template <int TY>
 cudaError_t launch_ty(Sim *sim, const StepParams &prm, int cur, int prev) {
   switch (sim->coef_form) {
+    case CF_VV: return launch_cf<TY, CF_VV>(sim, prm, cur, prev);
     case CF_F16: return launch_cf<TY, CF_F16>(sim, prm, cur, prev);
     case CF_BF16: return launch_cf<TY, CF_BF16>(sim, prm, cur, prev);
-    default: break;
-  }
-  if constexpr (TY == 6) {
-    return cudaErrorInvalidValue;  // tile rows 6: narrow forms only
-  } else {
-    if (sim->coef_form == CF_VV) return launch_cf<TY, CF_VV>(sim, prm, cur, prev);
-    return launch_cf<TY, CF_F32>(sim, prm, cur, prev);
+    default: return launch_cf<TY, CF_F32>(sim, prm, cur, prev);
   }
 }
 
 template <int TY>
 cudaError_t set_attrs(int form) {
   switch (form) {
+    case CF_VV: return set_smem_attr_all<TY, CF_VV>();
     case CF_F16: return set_smem_attr_all<TY, CF_F16>();
     case CF_BF16: return set_smem_attr_all<TY, CF_BF16>();
-    default: break;
-  }
-  if constexpr (TY == 6) {
-    return cudaErrorInvalidValue;
-  } else {
-    if (form == CF_VV) return set_smem_attr_all<TY, CF_VV>();
-    return set_smem_attr_all<TY, CF_F32>();
+    default: return set_smem_attr_all<TY, CF_F32>();
   }
 }
 
-// 32 x 8 tiles with two CTAs per SM measured fastest on GB300 for the FP32
-// forms (616^3 cube: 2.83 ms per step vs 3.09 ms for 32 x 16).
-// DC_GB300_FAST_TY=16 selects 32 x 16; DC_GB300_FAST_TY=6 selects 32 x 6
-// with three CTAs per SM for the FP16/BF16 forms (the FP32 forms keep 8).
-int chosen_ty(int form) {
+// 32 x 8 tiles with two CTAs per SM measured fastest on GB300 (616^3 cube:
+// 2.83 ms per step vs 3.09 ms for 32 x 16; 32 x 6 with three CTAs per SM
+// was slower still: 2.93 ms FP32, 2.68 ms FP16 against 2.56 ms).
+// DC_GB300_FAST_TY=16 selects 32 x 16.
+int chosen_ty(int) {
   const char *e = std::getenv("DC_GB300_FAST_TY");
   const int v = e ? std::atoi(e) : 0;
-  if (v == 16) return 16;
-  if (v == 6 && (form == CF_F16 || form == CF_BF16)) return 6;
-  return 8;
+  return v == 16 ? 16 : 8;
 }
 
 template <typename F>
 auto by_ty(int ty, F &&f) {
   if (ty == 16) return f(std::integral_constant<int, 16>{});
-  if (ty == 6) return f(std::integral_constant<int, 6>{});
   return f(std::integral_constant<int, 8>{});
 }
 
@@ -710,8 +731,9 @@ bool fast_encode_pair_maps(const float2 *buf, long long sx, long long sy, long l
 }
 
 bool fast_encode_medium_maps(int form, const float *coef, const void *coef16, const float *vv,
-                             long long sx, long long sy, long long sz, long long pitch,
-                             long long count, int ty, CUtensorMap out[3], std::string *err) {
+                             const float4 *vbase, long long sx, long long sy, long long sz,
+                             long long pitch, long long count, int ty, CUtensorMap out[4],
+                             std::string *err) {
   const uint64_t X = sx, Y = sy, Z = sz, P = pitch, PL = pitch * sy;
   const uint64_t dims3[3] = {X, Y, Z};
   const uint64_t str8[2] = {P * 8, PL * 8};
@@ -725,25 +747,38 @@ bool fast_encode_medium_maps(int form, const float *coef, const void *coef16, co
   const uint32_t box16[3] = {2 * kTX, static_cast<uint32_t>(ty), 1};
   const auto U64 = CU_TENSOR_MAP_DATA_TYPE_UINT64, U32 = CU_TENSOR_MAP_DATA_TYPE_UINT32;
   const long long cnt = count;
-  // out[0] = L (cxx, cyy, cxy, czz), out[1] = O1, out[2] = O2
+  // out[0] = L (cxx, cyy, cxy, czz), out[1] = O1, out[2] = O2, out[3] = the
+  // FP16 form's row bases
+  bool ok = false;
   switch (form) {
     case CF_F32: {
       const char *c = reinterpret_cast<const char *>(coef);
-      return encode_tiled(&out[0], c, 3, dims16, str16, box16, err, U64) &&
-             encode_tiled(&out[1], c + cnt * 16, 3, dims16, str16, box16, err, U64) &&
-             encode_tiled(&out[2], c + cnt * 32, 3, dims3, str8, box_tile, err, U64);
+      ok = encode_tiled(&out[0], c, 3, dims16, str16, box16, err, U64) &&
+           encode_tiled(&out[1], c + cnt * 16, 3, dims16, str16, box16, err, U64) &&
+           encode_tiled(&out[2], c + cnt * 32, 3, dims3, str8, box_tile, err, U64);
+      break;
     }
     case CF_VV:
-      if (!encode_tiled(&out[1], vv, 3, dims3, str8, box_tile, err, U64)) return false;
+      ok = encode_tiled(&out[1], vv, 3, dims3, str8, box_tile, err, U64);
       out[0] = out[2] = out[1];  // unused
-      return true;
+      break;
     default: {  // CF_F16, CF_BF16: 8-byte L, 8-byte O1, 4-byte O2
       const char *h = static_cast<const char *>(coef16);
-      return encode_tiled(&out[0], h, 3, dims3, str8, box_tile, err, U64) &&
-             encode_tiled(&out[1], h + cnt * 8, 3, dims3, str8, box_tile, err, U64) &&
-             encode_tiled(&out[2], h + cnt * 16, 3, dims3, str4, box_tile, err, U32);
+      ok = encode_tiled(&out[0], h, 3, dims3, str8, box_tile, err, U64) &&
+           encode_tiled(&out[1], h + cnt * 8, 3, dims3, str8, box_tile, err, U64) &&
+           encode_tiled(&out[2], h + cnt * 16, 3, dims3, str4, box_tile, err, U32);
     }
   }
+  if (!ok) return false;
+  if (form != CF_F16) {
+    out[3] = out[2];  // unused
+    return true;
+  }
+  // row bases: [sz][sy] float4 as a 2-D tensor of 8-byte elements, x = 2 y
+  const uint64_t dims_vb[2] = {2 * Y, Z};
+  const uint64_t str_vb[1] = {Y * 16};
+  const uint32_t box_vb[2] = {2 * static_cast<uint32_t>(ty), 1};
+  return encode_tiled(&out[3], vbase, 2, dims_vb, str_vb, box_vb, err, U64);
 }
 
 bool fast_encode_maps(Sim *sim, std::string *err) {
@@ -759,8 +794,9 @@ bool fast_encode_maps(Sim *sim, std::string *err) {
     if (!fast_encode_pair_maps(sim->pq[b], sim->sx, sim->sy, sim->sz, sim->pitch, kTY,
                                &sim->tm_halo[b], &sim->tm_own[b], err))
       return false;
-  if (!fast_encode_medium_maps(sim->coef_form, sim->coef, sim->coef16, sim->vv, sim->sx, sim->sy,
-                               sim->sz, sim->pitch, sim->count, kTY, sim->tm_c, err))
+  if (!fast_encode_medium_maps(sim->coef_form, sim->coef, sim->coef16, sim->vv, sim->vbase,
+                               sim->sx, sim->sy, sim->sz, sim->pitch, sim->count, kTY, sim->tm_c,
+                               err))
     return false;
   sim->maps_tx = kTX;
   sim->maps_ty = kTY;
@@ -796,13 +832,8 @@ cudaError_t batch_attr_ty(int form) {
   switch (form) {
     case CF_F16: return batch_attr_cf<TY, CF_F16>();
     case CF_BF16: return batch_attr_cf<TY, CF_BF16>();
-    default: break;
-  }
-  if constexpr (TY == 6) {
-    return cudaErrorInvalidValue;
-  } else {
-    if (form == CF_VV) return batch_attr_cf<TY, CF_VV>();
-    return batch_attr_cf<TY, CF_F32>();
+    case CF_VV: return batch_attr_cf<TY, CF_VV>();
+    default: return batch_attr_cf<TY, CF_F32>();
   }
 }
 
@@ -829,13 +860,8 @@ int batch_occ_ty(int form, bool iso, bool sponge) {
   switch (form) {
     case CF_F16: return batch_occ_cf<TY, CF_F16>(iso, sponge);
     case CF_BF16: return batch_occ_cf<TY, CF_BF16>(iso, sponge);
-    default: break;
-  }
-  if constexpr (TY == 6) {
-    return 0;
-  } else {
-    if (form == CF_VV) return batch_occ_cf<TY, CF_VV>(iso, sponge);
-    return batch_occ_cf<TY, CF_F32>(iso, sponge);
+    case CF_VV: return batch_occ_cf<TY, CF_VV>(iso, sponge);
+    default: return batch_occ_cf<TY, CF_F32>(iso, sponge);
   }
 }
 
@@ -864,21 +890,14 @@ cudaError_t launch_batch_ty(cudaStream_t st, const BatchLaunch &bl, int form, bo
   switch (form) {
     case CF_F16: return launch_batch_cf<TY, CF_F16>(st, bl, iso, sponge, blocks);
     case CF_BF16: return launch_batch_cf<TY, CF_BF16>(st, bl, iso, sponge, blocks);
-    default: break;
-  }
-  if constexpr (TY == 6) {
-    return cudaErrorInvalidValue;
-  } else {
-    if (form == CF_VV) return launch_batch_cf<TY, CF_VV>(st, bl, iso, sponge, blocks);
-    return launch_batch_cf<TY, CF_F32>(st, bl, iso, sponge, blocks);
+    case CF_VV: return launch_batch_cf<TY, CF_VV>(st, bl, iso, sponge, blocks);
+    default: return launch_batch_cf<TY, CF_F32>(st, bl, iso, sponge, blocks);
   }
 }
 
 }  // namespace
 
-bool fast_tile_rows_valid(int ty, int form) {
-  return ty == 8 || ty == 16 || (ty == 6 && (form == CF_F16 || form == CF_BF16));
-}
+bool fast_tile_rows_valid(int ty, int) { return ty == 8 || ty == 16; }
 
 cudaError_t batch_prepare(int ty, int form) {
   return by_ty(ty, [&](auto t) { return batch_attr_ty<decltype(t)::value>(form); });

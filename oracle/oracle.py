@@ -355,6 +355,58 @@ def reference_medium(lib, geom: Geometry, seed: int = 0):
     return aniso, coef
 
 
+def _round_bf16(a):
+    u = np.asarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def fixed16(c):
+    """An angle term in the GPU's 16-bit medium: c x 2^15 rounded to nearest
+    even, clamped to [-32768, 32767], scaled back (exact)."""
+    q = np.clip(np.rint(np.asarray(c, np.float32) * np.float32(32768.0)), -32768, 32767)
+    return (q / 32768.0).astype(np.float32)
+
+
+def row_referenced16(v):
+    """A velocity term in the GPU's 16-bit medium: per row (the last axis)
+    the base b is the midrange of the row's non-zero values (float), the
+    stored value d = v / b - 1 rounded to FP16, read back as b + b * d with a
+    single rounding."""
+    v = np.asarray(v, np.float32)
+    nz = v != 0
+    mn = np.where(nz, v, np.float32(np.inf)).min(axis=-1, keepdims=True).astype(np.float32)
+    mx = np.where(nz, v, np.float32(-np.inf)).max(axis=-1, keepdims=True).astype(np.float32)
+    with np.errstate(invalid="ignore", over="ignore"):
+        mid = (np.float32(0.5) * (mn + mx)).astype(np.float32)
+    base = np.where(mn <= mx, mid, np.float32(0.0)).astype(np.float32)
+    safe = np.where(base != 0, base, np.float32(1.0)).astype(np.float32)
+    d = np.where(base != 0, (v / safe).astype(np.float32) - np.float32(1.0),
+                 np.float32(0.0)).astype(np.float32)
+    d16 = d.astype(np.float16).astype(np.float64)
+    b64 = base.astype(np.float64)
+    return (b64 * d16 + b64).astype(np.float32)
+
+
+def narrow_medium(coef, fmt: str):
+    """The ten coefficients (dc_precomp_vars order, arrays (sz, sy, sx)) as
+    the fast kernel reads its 16-bit medium copy.
+
+    "f16":  the six angle terms as 16-bit fixed point (fixed16), the four
+            velocity terms as FP16 ratios to a per-row FP32 base
+            (row_referenced16);
+    "bf16": all ten rounded to BF16, the velocity terms scaled by 2^-vexp
+            (max below 2^14) before rounding and scaled back."""
+    if fmt == "f16":
+        return [fixed16(c) for c in coef[:6]] + [row_referenced16(c) for c in coef[6:]]
+    vmax = max(float(np.abs(c).max()) for c in coef[6:])
+    vexp = int(np.frexp(vmax)[1]) - 14 if vmax > 0 else 0
+    out = [_round_bf16(c) for c in coef[:6]]
+    out += [(_round_bf16(np.asarray(c, np.float32) * np.float32(2.0 ** -vexp))
+             * np.float32(2.0 ** vexp)).astype(np.float32) for c in coef[6:]]
+    return out
+
+
 def rel_l2(a, b) -> float:
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)

@@ -1,49 +1,32 @@
 """The mixed-precision medium forms (DC_GB300_MEDIUM_PRECOMP_F16 / _BF16):
-the fast kernel reads an FP16/BF16 copy of the ten coefficients (velocity
-terms scaled by 2^-vexp), computes in FP32 and keeps FP32 wavefields.
+the fast kernel reads a 16-bit copy of the ten coefficients, computes in
+FP32 and keeps FP32 wavefields.  The FP16 form stores the angle terms as
+16-bit fixed point and the velocity terms as FP16 ratios to a per-row FP32
+base; the BF16 form rounds all ten to BF16 (velocity terms scaled by
+2^-vexp).
 
 * Against the oracle run on identically rounded coefficients the result must
   agree to FP32 reordering noise (rel. L2 <= 1e-5): the kernel adds no error
   beyond the storage rounding.
 * Against the FP64 oracle on the exact coefficients, on a 64^3 + 16 layered
   medium after 300 steps of dt = 0.8 ms, FP16 storage meets the accuracy bar
-  of relative L2 <= 1e-3 (measured 7.3e-4).  BF16 storage does not: its 8
+  of relative L2 <= 1e-3 with room to spare (the CPU emulation of the same
+  encoding stays at 3.9e-4 after 1500 steps).  BF16 storage does not: its 8
   mantissa bits on the four velocity terms alone cost 4.4e-3 (all ten
   coefficients 4.7e-3); the test pins that it stays within (1e-3, 1e-2] so
   that the miss is stated, not hidden behind a loose bound.
 """
-import math
-
 import numpy as np
 import pytest
 
-from oracle.oracle import KIND_F32, KIND_F64, Geometry, rel_l2
+from oracle.oracle import KIND_F32, KIND_F64, Geometry, narrow_medium, rel_l2
 
 pytestmark = pytest.mark.gpu
 
 
-def round_f16(a):
-    return np.asarray(a, np.float32).astype(np.float16).astype(np.float32)
-
-
-def round_bf16(a):
-    u = np.asarray(a, np.float32).view(np.uint32).astype(np.uint64)
-    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
-    return u.astype(np.uint32).view(np.float32)
-
-
 def narrowed(coef, fmt):
-    """Coefficients as the fast kernel sees them: ch1d* rounded directly,
-    the velocity terms (dc_precomp_vars indices 6..9) scaled by 2^-vexp with
-    max < 2^14, rounded, scaled back (exact powers of two)."""
-    rnd = round_f16 if fmt == "f16" else round_bf16
-    vmax = max(float(np.abs(c).max()) for c in coef[6:])
-    _, e0 = math.frexp(vmax)
-    vexp = e0 - 14
-    out = [rnd(c) for c in coef[:6]]
-    out += [(rnd(c * np.float32(2.0 ** -vexp)) * np.float32(2.0 ** vexp)).astype(np.float32)
-            for c in coef[6:]]
-    return out
+    """Coefficients as the fast kernel sees them (oracle.narrow_medium)."""
+    return narrow_medium(coef, fmt)
 
 
 @pytest.fixture(scope="module")
@@ -108,14 +91,14 @@ def test_mixed_precision_keeps_fp32_for_exact_kernel(dc, port, layered_case):
     assert np.array_equal(out["pc"], ref.pc)
 
 
-@pytest.mark.parametrize("medium_form", [2, 3])
-def test_tile_rows_six_bit_identical(dc, layered_case, monkeypatch, medium_form):
-    """DC_GB300_FAST_TY=6 (32 x 6 tiles, three CTAs per SM) on the FP16/BF16
-    forms gives the same bits as the default 32 x 8 tiles."""
+@pytest.mark.parametrize("medium_form", [0, 2, 3])
+def test_tile_rows_sixteen_bit_identical(dc, layered_case, monkeypatch, medium_form):
+    """DC_GB300_FAST_TY=16 (32 x 16 tiles) gives the same bits as the default
+    32 x 8 tiles on the FP32, FP16 and BF16 coefficient forms."""
     geom, coef, steps, dt, src, sponge, s_idx, f64 = layered_case
     n = 60
     out = {}
-    for ty in ("8", "6"):
+    for ty in ("8", "16"):
         monkeypatch.setenv("DC_GB300_FAST_TY", ty)
         with dc.Simulation(geom.sizes, (12.5,) * 3, dt, kernel=dc.KERNEL_FAST,
                            medium=medium_form, device=0) as sim:
@@ -127,4 +110,4 @@ def test_tile_rows_six_bit_identical(dc, layered_case, monkeypatch, medium_form)
             sim.synchronize()
             out[ty] = sim.get_fields()
     for k in ("pp", "pc", "qp", "qc"):
-        assert np.array_equal(out["8"][k], out["6"][k]), k
+        assert np.array_equal(out["8"][k], out["16"][k]), k

@@ -1,15 +1,24 @@
-"""Why the wavefields stay FP32 (CPU, oracle emulation): on a layered
-medium, rounding p and q to FP16 (power-of-two scale per field) or BF16 at
-every store costs far more than the 1e-3 relative-L2 budget against the
-FP64 oracle, while FP16 storage of the coefficients alone stays inside it.
-The storage rounding is emulated by the oracle's store modes (the GPU
-kernels never store narrow wavefields)."""
+"""Storage precision on the CPU (oracle emulation), against the FP64
+oracle on a 40^3 + 8 layered medium after 200 steps of dt = 0.8 ms:
+
+* The FP16 medium copy the GPU reads -- angle terms as 16-bit fixed point,
+  velocity terms as FP16 ratios to a per-row FP32 base
+  (oracle.narrow_medium) -- costs over ten times less than rounding each
+  coefficient straight to FP16 under a per-field power-of-two scale: the
+  rounding of the velocity terms, which act as a perturbation of the
+  medium, is what the direct form pays for.
+* Rounding p and q to FP16 (power-of-two scale per field) or BF16 at every
+  store costs far more than the 1e-3 relative-L2 budget, which is why the
+  wavefields stay FP32.  The storage rounding is emulated by the oracle's
+  store modes (the GPU kernels never store narrow wavefields)."""
 import numpy as np
 
-from oracle.oracle import KIND_F32, KIND_F64, STORE_BF16, STORE_F16, Geometry, rel_l2
+from oracle.oracle import (KIND_F32, KIND_F64, STORE_BF16, STORE_F16, Geometry, narrow_medium,
+                           rel_l2)
 
 
-def _narrow_f16(coef):
+def _direct_f16(coef):
+    """Each coefficient rounded to FP16 under its own power-of-two scale."""
     out = []
     for c in coef:
         m = float(np.abs(c).max())
@@ -19,7 +28,7 @@ def _narrow_f16(coef):
     return out
 
 
-def test_narrow_wavefields_miss_the_accuracy_budget(dc, port):
+def test_medium_and_wavefield_storage_precision(dc, port):
     from dc_gb300 import medium
     g = Geometry((40, 40, 40), 8)
     coef = port.precomp(medium.layered_fields(medium.layered_spec(7, g.sizes), g.sizes))
@@ -30,15 +39,18 @@ def test_narrow_wavefields_miss_the_accuracy_budget(dc, port):
     z32 = lambda: [np.zeros(g.shape, np.float32) for _ in range(4)]  # noqa: E731
     f64 = port.run(KIND_F64, g.sizes, (12.5,) * 3, dt, steps,
                    *[np.zeros(g.shape, np.float64) for _ in range(4)], coef=coef, **common)
-    c16 = _narrow_f16(coef)
+    direct = port.run(KIND_F32, g.sizes, (12.5,) * 3, dt, steps, *z32(), coef=_direct_f16(coef),
+                      **common)
+    c16 = narrow_medium(coef, "f16")
     coef_only = port.run(KIND_F32, g.sizes, (12.5,) * 3, dt, steps, *z32(), coef=c16, **common)
     f16 = port.run(KIND_F32, g.sizes, (12.5,) * 3, dt, steps, *z32(), coef=c16, store=STORE_F16,
                    store_exp=(10, 10), **common)
     bf16 = port.run(KIND_F32, g.sizes, (12.5,) * 3, dt, steps, *z32(), coef=c16,
                     store=STORE_BF16, **common)
-    e_coef = rel_l2(coef_only.pc, f64.pc)
+    e_direct, e_coef = rel_l2(direct.pc, f64.pc), rel_l2(coef_only.pc, f64.pc)
     e_f16, e_bf16 = rel_l2(f16.pc, f64.pc), rel_l2(bf16.pc, f64.pc)
-    print(f"rel. L2 vs FP64 after {steps} steps: FP16 coefficients {e_coef:.2e}, "
-          f"+ FP16 wavefields {e_f16:.2e}, + BF16 wavefields {e_bf16:.2e}")
-    assert e_coef < 1e-3
+    print(f"rel. L2 vs FP64 after {steps} steps: direct FP16 coefficients {e_direct:.2e}, "
+          f"the GPU's FP16 medium {e_coef:.2e}, + FP16 wavefields {e_f16:.2e}, "
+          f"+ BF16 wavefields {e_bf16:.2e}")
+    assert e_coef < 1e-4 and e_coef < e_direct / 10
     assert e_f16 > 1e-3 and e_bf16 > 1e-2
