@@ -74,7 +74,11 @@ struct FastLayout {
   static constexpr int HX = TX + 2 * kHalo;
   static constexpr int HY = TY + 2 * kHalo;
   static constexpr int NT = TX * TY;
-  static constexpr int NSTAGE = 3;
+  // TMA ring depth: 4 stages for the FP32 ten-coefficient form (its 17 KB
+  // stages land later than the narrow forms'; 616^3 step 2.686 ms against
+  // 2.735 ms with 3), 3 for the others (the FP16 form measured 2.755 ms with
+  // 4 against 2.629 ms)
+  static constexpr int NSTAGE = CF == CF_F32 ? 4 : 3;
   static constexpr int HALO_BYTES = align128(HX * HY * 8);  // (p, q) pairs
   static constexpr int OFF_H = 0;
   static constexpr int OFF_L = HALO_BYTES;
@@ -89,9 +93,15 @@ struct FastLayout {
   static constexpr int OFF_DY = NSTAGE * STAGE_BYTES;         // 3 buffers
   // per-thread ring of the delayed in-plane terms of the last 9 planes:
   // (A_p, A_q, B_p, B_q) and czz
+  // delayed in-plane terms: 9 slots indexed by the compile-time plane
+  // number of the 9-plane unrolled body, or -- where the fourth TMA stage
+  // needs the room for two CTAs per SM -- the 5 slots the 4-plane delay
+  // needs, indexed at run time
+  static constexpr int RING = NSTAGE == 4 ? 5 : 9;
+  static_assert(RING == 9 || RING == 5, "ring slots");
   static constexpr int OFF_RA = OFF_DY + 3 * DY_BYTES;
-  static constexpr int OFF_RZ = OFF_RA + 9 * NT * 16;
-  static constexpr int OFF_BAR = OFF_RZ + 9 * NT * 4;
+  static constexpr int OFF_RZ = OFF_RA + RING * NT * 16;
+  static constexpr int OFF_BAR = OFF_RZ + RING * NT * 4;
   static constexpr int SMEM_BYTES = OFF_BAR + NSTAGE * 8;
   static constexpr uint32_t TX_HALO = HX * HY * 8u;
   static constexpr uint32_t TX_LEAD = NT * CB::L;
@@ -360,6 +370,13 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
   int abort_it = -1;
   float4 *ring_ab = reinterpret_cast<float4 *>(smem + Lay::OFF_RA);
   float *ring_czz = reinterpret_cast<float *>(smem + Lay::OFF_RZ);
+  constexpr int RING = Lay::RING;
+  int rw = 0;  // 5-slot ring: the slot of this iteration (it % 5)
+  // stage and parity of this iteration when the ring depth does not divide
+  // the 9-plane body (compile-time otherwise)
+  constexpr bool kStaticStage = 9 % NSTAGE == 0;
+  int stg = 0;
+  uint32_t sph = 0;
 
   // inactive threads of edge tiles may sit past the array: no profile read
   const float gxy = (SPONGE && active)
@@ -393,11 +410,15 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
     for (int u = 0; u < 9; ++u) {
       const int it = it0 + u;
       if (it < n_it) {  // CTA-uniform
-        // stage u % 3; its use count is it / 3 = 3 * (it0 / 9) + u / 3
-        unsigned char *st = smem + (u % 3) * Lay::STAGE_BYTES;
-        const bool ok = mbar_wait_bounded(&bars[u % 3],
-                                          mpar ^ static_cast<uint32_t>((u / 3) & 1),
-                                          kWaitLimitNs);
+        // stage it % NSTAGE; with NSTAGE dividing 9 its use count is
+        // it / NSTAGE = (9 / NSTAGE) * (it0 / 9) + u / NSTAGE
+        const int sidx = kStaticStage ? u % NSTAGE : stg;
+        const uint32_t spar =
+            kStaticStage
+                ? (((9 / NSTAGE) & 1 ? mpar : 0u) ^ static_cast<uint32_t>((u / NSTAGE) & 1))
+                : sph;
+        unsigned char *st = smem + sidx * Lay::STAGE_BYTES;
+        const bool ok = mbar_wait_bounded(&bars[sidx], spar, kWaitLimitNs);
         const float2 *h = reinterpret_cast<const float2 *>(st + Lay::OFF_H);
         float2 *dyb = reinterpret_cast<float2 *>(smem + Lay::OFF_DY + (u % 3) * Lay::DY_BYTES);
 
@@ -443,8 +464,9 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
           const float4 lc = load_lead<CF>(st + Lay::OFF_L, ot);  // cxx, cyy, cxy, czz
           const float2 av = fma2(bc(lc.z), xy, fma2(bc(lc.y), yy, mul2(bc(lc.x), xx)));
           const float2 bv = add2(xx, yy);
-          ring_ab[u * NT + ot] = make_float4(av.x, av.y, bv.x, bv.y);
-          ring_czz[u * NT + ot] = lc.w;
+          const int sw = RING == 9 ? u : rw;
+          ring_ab[sw * NT + ot] = make_float4(av.x, av.y, bv.x, bv.y);
+          ring_czz[sw * NT + ot] = lc.w;
         }
 
         // ---- output plane z = k - 4
@@ -453,8 +475,10 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
           const int m4 = (u + 1) % 9, m3 = (u + 2) % 9, m2 = (u + 3) % 9,
                     m1 = (u + 4) % 9, c = (u + 5) % 9, p1 = (u + 6) % 9,
                     p2 = (u + 7) % 9, p3 = (u + 8) % 9, p4 = u;
-          const float4 ab = ring_ab[c * NT + ot];  // A, B of plane z
-          const float czz = ring_czz[c * NT + ot];
+          // slot of plane z = k - 4, written four iterations ago
+          const int sr = RING == 9 ? c : (rw == 4 ? 0 : rw + 1);
+          const float4 ab = ring_ab[sr * NT + ot];  // A, B of plane z
+          const float czz = ring_czz[sr * NT + ot];
           const float2 zz = d2s<ISO, CHAIN>(w2z, cq[c], cq[m1], cq[p1], cq[m2], cq[p2], cq[m3],
                                cq[p3], cq[m4], cq[p4]);
           const float2 xz = d1s<ISO, CHAIN>(w1z, dxq[m1], dxq[p1], dxq[m2], dxq[p2],
@@ -510,6 +534,11 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
             *out = nv;
           }
           out += prm.plane;
+        }
+        if (RING != 9) rw = rw == 4 ? 0 : rw + 1;
+        if (!kStaticStage && ++stg == NSTAGE) {
+          stg = 0;
+          sph ^= 1u;
         }
       }
     }
