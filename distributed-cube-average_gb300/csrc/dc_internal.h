@@ -172,6 +172,7 @@ struct Sim {
   int config_version = 0;
   // tensor maps for the fast kernel (encoded for one tile shape)
   CUtensorMap tm_halo[2], tm_own[2], tm_c[4];  // tm_c: L, O1, O2, row bases
+  bool deep_ring = false;  // fast FP32 sweep with the 4-stage TMA ring
   int maps_tx = 0, maps_ty = 0;
   // learned absorbing layer, applied after every stencil pass of a run
   const float *lb_params = nullptr;  // MLP compute parameters (device, owned by the MLP)

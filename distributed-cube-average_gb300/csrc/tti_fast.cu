@@ -68,17 +68,17 @@ struct CoefBytes {
   static constexpr int O2 = CF == CF_F32 ? 8 : CF == CF_VV ? 0 : 4;
 };
 
-template <int TX, int TY, int CF>
+template <int TX, int TY, int CF, int NS = 3>
 struct FastLayout {
   using CB = CoefBytes<CF>;
   static constexpr int HX = TX + 2 * kHalo;
   static constexpr int HY = TY + 2 * kHalo;
   static constexpr int NT = TX * TY;
-  // TMA ring depth: 4 stages for the FP32 ten-coefficient form (its 17 KB
-  // stages land later than the narrow forms'; 616^3 step 2.686 ms against
-  // 2.735 ms with 3), 3 for the others (the FP16 form measured 2.755 ms with
-  // 4 against 2.629 ms)
-  static constexpr int NSTAGE = CF == CF_F32 ? 4 : 3;
+  // TMA ring depth: 3, or 4 for large FP32 ten-coefficient boxes (their
+  // 17 KB stages land late when the whole GPU streams from DRAM; see
+  // fast_encode_maps)
+  static constexpr int NSTAGE = NS;
+  static_assert(NS == 3 || NS == 4, "ring depth");
   static constexpr int HALO_BYTES = align128(HX * HY * 8);  // (p, q) pairs
   static constexpr int OFF_H = 0;
   static constexpr int OFF_L = HALO_BYTES;
@@ -290,7 +290,7 @@ __device__ __forceinline__ OutMedium load_out(const unsigned char *o1, const uns
 // they feed the arithmetic directly).
 // Returns false if a TMA wait timed out: the error word is set and the
 // copies in flight have been given a bounded chance to land.
-template <int TX, int TY, int CF, bool SPONGE, bool ISO>
+template <int TX, int TY, int CF, bool SPONGE, bool ISO, int NS>
 __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
                                              const CUtensorMap *tm_prev,
                                              const CUtensorMap *tm_l,
@@ -299,7 +299,7 @@ __device__ __forceinline__ bool sweep_column(const CUtensorMap *tm_cur,
                                              const CUtensorMap *tm_vb, const StepParams &prm,
                                              const StepParams &cw, const int x0, const int y0, const int zb,
                                              const int ze, unsigned char *smem) {
-  using Lay = FastLayout<TX, TY, CF>;
+  using Lay = FastLayout<TX, TY, CF, NS>;
   using CB = CoefBytes<CF>;
   constexpr int NSTAGE = Lay::NSTAGE;
   constexpr int HX = Lay::HX;
@@ -591,7 +591,7 @@ constexpr int kMinBlocks = NT <= 256 ? 2 : 1;
 // kernels refuse to run otherwise (CTA-uniform, before any copy is issued).
 
 // One pass over a box: CTA (bx, by, bz) sweeps tile (bx, by), z-chunk bz.
-template <int TX, int TY, int CF, bool SPONGE, bool ISO>
+template <int TX, int TY, int CF, bool SPONGE, bool ISO, int NS>
 __global__ void __launch_bounds__(TX *TY, kMinBlocks<TX * TY>)
     fast_kernel(const __grid_constant__ CUtensorMap tm_cur,
                 const __grid_constant__ CUtensorMap tm_prev,
@@ -609,8 +609,8 @@ __global__ void __launch_bounds__(TX *TY, kMinBlocks<TX * TY>)
   const int y0 = prm.tile_y0 + static_cast<int>(blockIdx.y) * TY;
   const int zb = prm.z0 + static_cast<int>(blockIdx.z) * prm.zchunk;
   const int ze = min(zb + prm.zchunk, prm.z1);
-  sweep_column<TX, TY, CF, SPONGE, ISO>(&tm_cur, &tm_prev, &tm_l, &tm_o1, &tm_o2, &tm_vb, prm,
-                                        prm, x0, y0, zb, ze, smem);
+  sweep_column<TX, TY, CF, SPONGE, ISO, NS>(&tm_cur, &tm_prev, &tm_l, &tm_o1, &tm_o2, &tm_vb,
+                                            prm, prm, x0, y0, zb, ze, smem);
 }
 
 // One step of a batch of shots: persistent CTAs stride over the work items
@@ -641,7 +641,7 @@ __global__ void __launch_bounds__(TX *TY, kMinBlocks<TX * TY>)
     const CUtensorMap *m = bl.maps + 4 * s;
     // weights, dt2 and energy (none) are the same in every shot: read them
     // from shot 0 at fixed offsets
-    if (!sweep_column<TX, TY, CF, SPONGE, ISO>(m + bl.cur_buf, m + 2 + (1 - bl.cur_buf),
+    if (!sweep_column<TX, TY, CF, SPONGE, ISO, 3>(m + bl.cur_buf, m + 2 + (1 - bl.cur_buf),
                                              &bl.tm_l, &bl.tm_o1, &bl.tm_o2, &bl.tm_vb, prm,
                                              bl.shot[0],
                                              x0, y0, zb, ze, smem))
@@ -650,13 +650,14 @@ __global__ void __launch_bounds__(TX *TY, kMinBlocks<TX * TY>)
 }
 
 // Compiled tile shapes: TX = 32 (one warp per tile row) and TY = 8 or 16
-// rows (256 or 512 threads), a 3-stage TMA ring.
+// rows (256 or 512 threads); a 3-stage TMA ring, or 4 stages for large
+// FP32 boxes.
 constexpr int kTX = 32;
 
-template <int TY, int CF, bool SPONGE, bool ISO>
+template <int TY, int CF, bool SPONGE, bool ISO, int NS>
 cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int cur_buf, int prev_buf) {
-  using Lay = FastLayout<kTX, TY, CF>;
-  auto kern = fast_kernel<kTX, TY, CF, SPONGE, ISO>;
+  using Lay = FastLayout<kTX, TY, CF, NS>;
+  auto kern = fast_kernel<kTX, TY, CF, SPONGE, ISO, NS>;
   const int nx = prm.x1 - prm.tile_x0, ny = prm.y1 - prm.tile_y0;
   const int nz = prm.z1 - prm.z0;
   dim3 grid((nx + kTX - 1) / kTX, (ny + TY - 1) / TY, (nz + prm.zchunk - 1) / prm.zchunk);
@@ -666,28 +667,43 @@ cudaError_t launch_fast_t(Sim *sim, const StepParams &prm, int cur_buf, int prev
   return cudaGetLastError();
 }
 
-template <int TY, int CF>
-cudaError_t set_smem_attr_all() {
-  using Lay = FastLayout<kTX, TY, CF>;
+template <int TY, int CF, int NS>
+cudaError_t set_smem_attr_ns() {
+  using Lay = FastLayout<kTX, TY, CF, NS>;
   cudaError_t e = cudaSuccess;
   const int b = Lay::SMEM_BYTES;
   const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, false, false>, attr, b);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, false, true>, attr, b);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, true, false>, attr, b);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, true, true>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, false, false, NS>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, false, true, NS>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, true, false, NS>, attr, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fast_kernel<kTX, TY, CF, true, true, NS>, attr, b);
   return e;
 }
 
 template <int TY, int CF>
-cudaError_t launch_cf(Sim *sim, const StepParams &prm, int cur, int prev) {
+cudaError_t set_smem_attr_all() {
+  cudaError_t e = set_smem_attr_ns<TY, CF, 3>();
+  if constexpr (CF == CF_F32)
+    if (e == cudaSuccess) e = set_smem_attr_ns<TY, CF, 4>();
+  return e;
+}
+
+template <int TY, int CF, int NS>
+cudaError_t launch_cf_ns(Sim *sim, const StepParams &prm, int cur, int prev) {
   const bool sp = prm.sponge != nullptr;
   const bool iso = sim->dx == sim->dy && sim->dy == sim->dz;
   if (sp)
-    return iso ? launch_fast_t<TY, CF, true, true>(sim, prm, cur, prev)
-               : launch_fast_t<TY, CF, true, false>(sim, prm, cur, prev);
-  return iso ? launch_fast_t<TY, CF, false, true>(sim, prm, cur, prev)
-             : launch_fast_t<TY, CF, false, false>(sim, prm, cur, prev);
+    return iso ? launch_fast_t<TY, CF, true, true, NS>(sim, prm, cur, prev)
+               : launch_fast_t<TY, CF, true, false, NS>(sim, prm, cur, prev);
+  return iso ? launch_fast_t<TY, CF, false, true, NS>(sim, prm, cur, prev)
+             : launch_fast_t<TY, CF, false, false, NS>(sim, prm, cur, prev);
+}
+
+template <int TY, int CF>
+cudaError_t launch_cf(Sim *sim, const StepParams &prm, int cur, int prev) {
+  if constexpr (CF == CF_F32)
+    if (sim->deep_ring) return launch_cf_ns<TY, CF, 4>(sim, prm, cur, prev);
+  return launch_cf_ns<TY, CF, 3>(sim, prm, cur, prev);
 }
 
 template <int TY>
@@ -810,7 +826,23 @@ bool fast_encode_medium_maps(int form, const float *coef, const void *coef16, co
   return encode_tiled(&out[3], vbase, 2, dims_vb, str_vb, box_vb, err, U64);
 }
 
+// The 4-stage ring pays off on large FP32 boxes, where the whole GPU
+// streams from DRAM over long sweeps (616^3: 2.690 ms per step against
+// 2.739 ms), and costs on small ones (the run-time ring indices add 10 %
+// instructions; 304^3: 411 against 371 us).  DC_GB300_FAST_STAGES=3|4
+// overrides the choice.
+constexpr long long kDeepRingPoints = 96ll << 20;
+
+bool deep_ring_for(const Sim *sim) {
+  if (sim->coef_form != CF_F32) return false;
+  const char *e = std::getenv("DC_GB300_FAST_STAGES");
+  if (e && std::atoi(e) == 3) return false;
+  if (e && std::atoi(e) == 4) return true;
+  return (sim->sx - 8) * (sim->sy - 8) * (sim->sz - 8) >= kDeepRingPoints;
+}
+
 bool fast_encode_maps(Sim *sim, std::string *err) {
+  sim->deep_ring = deep_ring_for(sim);
   // dynamic shared memory above 48 KB must be enabled per kernel and device
   // (done here, before any stream capture)
   const int kTY = chosen_ty(sim->coef_form);

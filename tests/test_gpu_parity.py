@@ -427,3 +427,20 @@ def test_observed_state_excludes_next_source(dc, port, kernel):
         sim.synchronize()
         f = sim.get_fields()
         assert rel_l2(f["pc"], ref2.pc) <= tol and rel_l2(f["qc"], ref2.qc) <= tol
+
+
+def test_fast_ring_depth_bit_identical(dc, monkeypatch):
+    """The FP32 sweep's 4-stage TMA ring (chosen for large boxes) gives the
+    same bits as the 3-stage ring: only the pipelining differs."""
+    g = load("hetero")
+    sizes = tuple(int(v) for v in g["sizes"])
+    coef = [g[f"coef{k}"] for k in range(10)]
+    out = {}
+    for ns in ("3", "4"):
+        monkeypatch.setenv("DC_GB300_FAST_STAGES", ns)
+        out[ns] = run_sim(dc, sizes, tuple(g["d"]), float(g["dt"]), int(g["steps"]),
+                          dc.KERNEL_FAST, 0, coef=coef, src_index=int(g["src_index"]),
+                          src=g["src"])
+    for k in ("pp", "pc", "qp", "qc"):
+        assert np.array_equal(out["3"][k], out["4"][k]), k
+    assert rel_l2(out["4"]["pc"], g["omp_pc"]) <= 1e-5
