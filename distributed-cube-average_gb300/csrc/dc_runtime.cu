@@ -1771,6 +1771,15 @@ extern "C" int dc_gb300_exact_steps_noalloc(const dc_gb300_config *cfg, float *p
   if (major != 10 || minor != 3)
     return dcg::fail(DC_GB300_ERR_DEVICE, "this build targets sm_103a");
   if (cudaSetDevice(dev) != cudaSuccess) return dcg::fail(DC_GB300_ERR_CUDA, "cudaSetDevice");
+  // every call synchronises its stream and reads the energy back, neither
+  // of which a capture allows: refuse before touching the capture
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap) != cudaSuccess ||
+      cap != cudaStreamCaptureStatusNone) {
+    cudaSetDevice(prev_dev);
+    return dcg::fail(DC_GB300_ERR_ARG,
+                     "dc_gb300_exact_steps_noalloc cannot run on a capturing stream");
+  }
   const int rc = run_steps(cfg, dev, pairs, medium, steps, energy,
                            static_cast<cudaStream_t>(stream));
   cudaSetDevice(prev_dev);

@@ -545,9 +545,11 @@ int dc_gb300_lb_rollout(dc_gb300_sim *wide, dc_gb300_sim *thin, const long offse
  *
  * The only device memory used besides the caller's buffers is a fixed
  * 33 KB file-scope scratch array per device (per-step energy accumulators
- * and a step counter).  The first call on a device looks up its address
- * (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  The address is kept for the life of the process: a
+ * and a step counter).  Every call synchronises `stream` and reads the
+ * energy back, so no call may run while a stream capture is active: a call
+ * on a capturing stream fails with DC_GB300_ERR_ARG and leaves the capture
+ * untouched.  The first call on a device looks up the scratch address
+ * (cudaGetSymbolAddress); it is kept for the life of the process: a
  * cudaDeviceReset between calls is not supported.  Each call clears the
  * part of the scratch it uses; all calls on a device share it, so calls
  * that overlap on the GPU race. */

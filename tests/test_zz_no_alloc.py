@@ -168,3 +168,30 @@ def test_noalloc_rejects_steps_beyond_scratch(dc):
     assert rc == dc.ERR_ARG
     msg = lib.dc_gb300_last_error().decode()
     assert "4096" in msg and "maximum" in msg
+
+
+def test_noalloc_refuses_capturing_stream(dc):
+    """A call on a stream under capture fails with DC_GB300_ERR_ARG before it
+    issues any work, and the caller's capture stays valid."""
+    torch = pytest.importorskip("torch")
+    sizes, d, dt, _, _ = _inputs("precomp")
+    cfg = _config(dc, sizes, d, dt, dc.MEDIUM_PRECOMP)
+    dummy = (C.c_void_p * 2)(16, 32)  # never dereferenced: the capture is checked first
+    lib = dc.lib()
+    x = torch.zeros(1, device="cuda:0")
+    stream = torch.cuda.Stream(device=0)
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        graph.capture_begin()
+        try:
+            x.add_(1.0)
+            rc = lib.dc_gb300_exact_steps_noalloc(C.byref(cfg), dummy, C.c_void_p(48), 1, None,
+                                                  C.c_void_p(stream.cuda_stream))
+        finally:
+            graph.capture_end()
+    assert rc == dc.ERR_ARG
+    assert "capturing" in lib.dc_gb300_last_error().decode()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert float(x.item()) == 1.0
