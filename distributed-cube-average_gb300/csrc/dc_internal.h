@@ -173,6 +173,7 @@ struct Sim {
   // tensor maps for the fast kernel (encoded for one tile shape)
   CUtensorMap tm_halo[2], tm_own[2], tm_c[4];  // tm_c: L, O1, O2, row bases
   bool deep_ring = false;  // fast FP32 sweep with the 4-stage TMA ring
+  int fast_slots = 0;      // fast-sweep CTAs resident on the device at once
   int maps_tx = 0, maps_ty = 0;
   // learned absorbing layer, applied after every stencil pass of a run
   const float *lb_params = nullptr;  // MLP compute parameters (device, owned by the MLP)
@@ -195,7 +196,8 @@ struct Sim {
 struct FastShape {
   int tx, ty, zchunk;
 };
-FastShape fast_shape(const Sim *sim);
+// Tile shape and z-chunk of a fast pass over an nx x ny x nz box.
+FastShape fast_shape(const Sim *sim, long long nx, long long ny, long long nz);
 bool fast_encode_maps(Sim *sim, std::string *err);
 // Tile rows (TY) of the fast kernel for coefficient form `form`: 8 unless
 // DC_GB300_FAST_TY selects 16.

@@ -227,7 +227,9 @@ StepParams make_params(Sim *s, const long long b0[3], const long long b1[3],
   p.z1 = static_cast<int>(b1[2]);
   p.tile_x0 = p.x0 & ~3;
   p.tile_y0 = p.y0;
-  p.zchunk = s->kernel == DC_GB300_KERNEL_FAST ? fast_shape(s).zchunk : kExactZChunk;
+  p.zchunk = s->kernel == DC_GB300_KERNEL_FAST
+                 ? fast_shape(s, p.x1 - p.tile_x0, p.y1 - p.tile_y0, p.z1 - p.z0).zchunk
+                 : kExactZChunk;
   p.pitch = s->pitch;
   p.plane = s->plane;
   fill_weights(&p, dx, dy, dz, dt);

@@ -88,7 +88,8 @@ def thin_sim(setup: Setup, device=0, kernel=KERNEL_FAST):
                      medium=MEDIUM_PRECOMP, device=device)
     sim.generate_layered(_origin_spec(setup, setup.offset))
     sim.set_fields()
-    sim.set_sponge(*_sponge(setup.thin_sizes, setup.layer, setup.thin_kappa))
+    if setup.thin_kappa > 0:  # a zero-strength profile is all ones: no sponge pass at all
+        sim.set_sponge(*_sponge(setup.thin_sizes, setup.layer, setup.thin_kappa))
     return sim
 
 
