@@ -444,3 +444,27 @@ def test_fast_ring_depth_bit_identical(dc, monkeypatch):
     for k in ("pp", "pc", "qp", "qc"):
         assert np.array_equal(out["3"][k], out["4"][k]), k
     assert rel_l2(out["4"]["pc"], g["omp_pc"]) <= 1e-5
+
+
+@pytest.mark.parametrize("stages", ["3", "4"])
+def test_fast_zchunks_bit_identical(dc, port, monkeypatch, stages):
+    """Splitting each column's z sweep into chunks (the count the wave model
+    picks, or any forced count) changes which CTA computes a plane, not how:
+    on the config-1 geometry (104^3, 96 updated planes) the fields are the
+    same bits for the default and for 1, 2, 3 and 5 chunks."""
+    geom = Geometry((64, 64, 64), 16)
+    aniso, coef = reference_medium(port, geom)
+    steps, dt, d = 40, 1e-3, (12.5, 12.5, 12.5)
+    src = port.source_table(dt, steps)
+    monkeypatch.setenv("DC_GB300_FAST_STAGES", stages)
+    out = {}
+    for chunks in (None, "1", "2", "3", "5"):
+        if chunks is None:
+            monkeypatch.delenv("DC_GB300_FAST_ZCHUNKS", raising=False)
+        else:
+            monkeypatch.setenv("DC_GB300_FAST_ZCHUNKS", chunks)
+        out[chunks] = run_sim(dc, geom.sizes, d, dt, steps, dc.KERNEL_FAST, 0, coef=coef,
+                              src_index=geom.source_index, src=src)
+    for chunks in ("1", "2", "3", "5"):
+        for k in ("pp", "pc", "qp", "qc"):
+            assert np.array_equal(out[None][k], out[chunks][k]), (chunks, k)
