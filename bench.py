@@ -650,8 +650,11 @@ def run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_ms, worl
     b0 = (4, 4, 4)
     b1 = (sx - 4, sy - 4, sz - 4)
 
+    marks = {}
+
     def abi_run(steps):
-        data = dc.device_data_init(proc)
+        data = dc.device_data_init(proc)  # returns once the arrays are on the device
+        marks["init"] = time.perf_counter()
         for it in range(steps):
             dc.device_add_source(data, src_idx, amp[it])
             dc.propagate(b0, b1, sizes, data, DX, DX, DX, DT)
@@ -671,12 +674,15 @@ def run_e2e(dc, torch, geom, args, src_idx, kernel, local, barrier, max_ms, worl
     data = abi_run(args.steps)
     el = time.perf_counter() - t0
     dc.device_data_free(data)
+    init_s, local_s = marks["init"] - t0, el  # this rank's phases
     el = max_ms(el)
     h2d = 14 * sx * sy * sz * 4
     d2h = 2 * sx * sy * sz * 4
     return {"value": pts * args.steps * world / el / 1e9, "unit": UNIT,
             "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-            "seconds": el, "api": "reference C ABI (dc_device_data_init, dc_device_add_source, "
+            "seconds": el,
+            "phases_s": {"init_and_upload": init_s, "steps_and_read_back": local_s - init_s},
+            "api": "reference C ABI (dc_device_data_init, dc_device_add_source, "
                                   "dc_propagate, dc_device_swap_arrays, "
                                   "dc_device_data_get_results), pinned host buffers"}
 
