@@ -111,3 +111,30 @@ def test_tile_rows_sixteen_bit_identical(dc, layered_case, monkeypatch, medium_f
             out[ty] = sim.get_fields()
     for k in ("pp", "pc", "qp", "qc"):
         assert np.array_equal(out["8"][k], out["16"][k]), k
+
+
+@pytest.mark.parametrize("medium_form", [0, 2, 3])
+def test_zchunks_bit_identical_narrow_media(dc, layered_case, monkeypatch, medium_form):
+    """z-chunks on the FP32, FP16 and BF16 coefficient forms: 1, 2, 3 and 5
+    chunks per column (each chunk's first output plane loads its own row
+    bases and delay-ring warm-up) give the same bits as the default count."""
+    geom, coef, steps, dt, src, sponge, s_idx, f64 = layered_case
+    n = 40
+    out = {}
+    for chunks in (None, "1", "2", "3", "5"):
+        if chunks is None:
+            monkeypatch.delenv("DC_GB300_FAST_ZCHUNKS", raising=False)
+        else:
+            monkeypatch.setenv("DC_GB300_FAST_ZCHUNKS", chunks)
+        with dc.Simulation(geom.sizes, (12.5,) * 3, dt, kernel=dc.KERNEL_FAST,
+                           medium=medium_form, device=0) as sim:
+            sim.set_precomp(coef)
+            sim.set_fields()
+            sim.set_source(s_idx, src)
+            sim.set_sponge(*sponge)
+            sim.run(n)
+            sim.synchronize()
+            out[chunks] = sim.get_fields()
+    for chunks in ("1", "2", "3", "5"):
+        for k in ("pp", "pc", "qp", "qc"):
+            assert np.array_equal(out[None][k], out[chunks][k]), (chunks, k)

@@ -446,15 +446,18 @@ def test_fast_ring_depth_bit_identical(dc, monkeypatch):
     assert rel_l2(out["4"]["pc"], g["omp_pc"]) <= 1e-5
 
 
-@pytest.mark.parametrize("stages", ["3", "4"])
-def test_fast_zchunks_bit_identical(dc, port, monkeypatch, stages):
+@pytest.mark.parametrize("stages,case", [("3", "cube"), ("4", "cube"), ("3", "ragged")])
+def test_fast_zchunks_bit_identical(dc, port, monkeypatch, stages, case):
     """Splitting each column's z sweep into chunks (the count the wave model
     picks, or any forced count) changes which CTA computes a plane, not how:
-    on the config-1 geometry (104^3, 96 updated planes) the fields are the
-    same bits for the default and for 1, 2, 3 and 5 chunks."""
-    geom = Geometry((64, 64, 64), 16)
+    on the config-1 geometry (104^3, 96 updated planes) and on a ragged box
+    with unequal spacings (run-time weights) the fields are the same bits
+    for the default and for 1, 2, 3 and 5 chunks."""
+    if case == "cube":
+        geom, steps, dt, d = Geometry((64, 64, 64), 16), 40, 1e-3, (12.5, 12.5, 12.5)
+    else:
+        geom, steps, dt, d = Geometry((37, 29, 53), 8), 40, 5e-4, (12.5, 10.0, 15.0)
     aniso, coef = reference_medium(port, geom)
-    steps, dt, d = 40, 1e-3, (12.5, 12.5, 12.5)
     src = port.source_table(dt, steps)
     monkeypatch.setenv("DC_GB300_FAST_STAGES", stages)
     out = {}
@@ -465,6 +468,7 @@ def test_fast_zchunks_bit_identical(dc, port, monkeypatch, stages):
             monkeypatch.setenv("DC_GB300_FAST_ZCHUNKS", chunks)
         out[chunks] = run_sim(dc, geom.sizes, d, dt, steps, dc.KERNEL_FAST, 0, coef=coef,
                               src_index=geom.source_index, src=src)
+    assert np.isfinite(out[None]["pc"]).all() and np.abs(out[None]["pc"]).max() > 0
     for chunks in ("1", "2", "3", "5"):
         for k in ("pp", "pc", "qp", "qc"):
             assert np.array_equal(out[None][k], out[chunks][k]), (chunks, k)
