@@ -368,11 +368,12 @@ def fixed16(c):
     return (q / 32768.0).astype(np.float32)
 
 
-def row_referenced16(v):
+def row_referenced16(v, ratio: str = "f16"):
     """A velocity term in the GPU's 16-bit medium: per row (the last axis)
     the base b is the midrange of the row's non-zero values (float), the
-    stored value d = v / b - 1 rounded to FP16, read back as b + b * d with a
-    single rounding."""
+    stored value d = v / b - 1 rounded to FP16 (ratio "f16", what the GPU
+    stores) or BF16 (ratio "bf16", a measured alternative), read back as
+    b + b * d with a single rounding."""
     v = np.asarray(v, np.float32)
     nz = v != 0
     mn = np.where(nz, v, np.float32(np.inf)).min(axis=-1, keepdims=True).astype(np.float32)
@@ -383,7 +384,7 @@ def row_referenced16(v):
     safe = np.where(base != 0, base, np.float32(1.0)).astype(np.float32)
     d = np.where(base != 0, (v / safe).astype(np.float32) - np.float32(1.0),
                  np.float32(0.0)).astype(np.float32)
-    d16 = d.astype(np.float16).astype(np.float64)
+    d16 = (d.astype(np.float16) if ratio == "f16" else _round_bf16(d)).astype(np.float64)
     b64 = base.astype(np.float64)
     return (b64 * d16 + b64).astype(np.float32)
 
@@ -396,9 +397,13 @@ def narrow_medium(coef, fmt: str):
             velocity terms as FP16 ratios to a per-row FP32 base
             (row_referenced16);
     "bf16": all ten rounded to BF16, the velocity terms scaled by 2^-vexp
-            (max below 2^14) before rounding and scaled back."""
+            (max below 2^14) before rounding and scaled back;
+    "bf16_rowref": the "f16" encoding with BF16 velocity ratios (not a GPU
+            form: the measured reason the BF16 copy cannot borrow it)."""
     if fmt == "f16":
         return [fixed16(c) for c in coef[:6]] + [row_referenced16(c) for c in coef[6:]]
+    if fmt == "bf16_rowref":
+        return [fixed16(c) for c in coef[:6]] + [row_referenced16(c, "bf16") for c in coef[6:]]
     vmax = max(float(np.abs(c).max()) for c in coef[6:])
     vexp = int(np.frexp(vmax)[1]) - 14 if vmax > 0 else 0
     out = [_round_bf16(c) for c in coef[:6]]

@@ -54,3 +54,30 @@ def test_medium_and_wavefield_storage_precision(dc, port):
           f"+ BF16 wavefields {e_bf16:.2e}")
     assert e_coef < 1e-4 and e_coef < e_direct / 10
     assert e_f16 > 1e-3 and e_bf16 > 1e-2
+
+
+def test_bf16_ratios_cost_four_times_the_fp16_ratios(dc, port):
+    """The FP16 form's encoding does not carry over to BF16: with the angle
+    terms in 16-bit fixed point in both, BF16 velocity ratios to the per-row
+    bases cost about four times the FP16 ratios against the FP64 oracle
+    (40^3 + 8, 600 steps; on 64^3 + 16 after 1500 steps the BF16 ratios
+    reach 1.3e-3, over the 1e-3 bar, and the FP16 ones 3.8e-4)."""
+    from dc_gb300 import medium
+    g = Geometry((40, 40, 40), 8)
+    coef = port.precomp(medium.layered_fields(medium.layered_spec(7, g.sizes), g.sizes))
+    steps, dt = 600, 0.8e-3
+    common = dict(src_index=g.index(g.sizes[0] // 2, g.sizes[1] // 2, 4 + 8 + 10),
+                  src=port.source_table(dt, steps, 60.0),
+                  sponge=[port.sponge_profile(s, 8, 0.35) for s in g.sizes])
+    z32 = lambda: [np.zeros(g.shape, np.float32) for _ in range(4)]  # noqa: E731
+    f64 = port.run(KIND_F64, g.sizes, (12.5,) * 3, dt, steps,
+                   *[np.zeros(g.shape, np.float64) for _ in range(4)], coef=coef, **common)
+    err = {}
+    for fmt in ("f16", "bf16_rowref"):
+        r = port.run(KIND_F32, g.sizes, (12.5,) * 3, dt, steps, *z32(),
+                     coef=narrow_medium(coef, fmt), **common)
+        err[fmt] = rel_l2(r.pc, f64.pc)
+    print(f"rel. L2 vs FP64 after {steps} steps: FP16 ratios {err['f16']:.2e}, "
+          f"BF16 ratios {err['bf16_rowref']:.2e}")
+    assert err["f16"] < 3e-4
+    assert err["bf16_rowref"] > 3 * err["f16"]
